@@ -1,0 +1,357 @@
+"""Benchmark of the Viola-Jones data-parallel path on GB300.
+
+Workload (a "step"): the full stage training step on 10,000 positive and
+10,000 negative synthetic 24x24 patches (seed 1): integral images, per-feature
+sort of all 162,336 Basic features (kept resident for the stage), then 50
+boosting rounds, each = best-weak search (bit-exact picks of the reference's
+search) + FP64 AdaBoost update + stage calibration.
+
+metric "stump GB/s": 20 bytes per (feature, sample) per round (f32 key write
++ read, sorted (f32 key, u16 index) pair write + read: one materialisation of
+the sort-based algorithm) x 162,336 x 20,000 x 50 / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  Under torchrun (N > 1) every rank runs its own
+replica of the step ("replicas only"; scaling "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NPOS = NNEG = 10000
+ROUNDS = 50
+SEED = 1
+BYTES_PER_ELEM_ROUND = 20  # algorithmic model of the stump search
+METRIC = "stump GB/s"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- GPU arm
+class Stage:
+    """Device-resident stage-training state for one step."""
+
+    def __init__(self, torch, V, patches, pool):
+        self.torch, self.V = torch, V
+        n = len(patches)
+        self.n = n
+        self.numPos = NPOS
+        self.d_p = torch.from_numpy(patches).cuda()
+        self.sumT = torch.empty(625 * n, dtype=torch.int32, device="cuda")
+        self.inv = torch.empty(n, dtype=torch.float32, device="cuda")
+        labels = np.array([1] * NPOS + [-1] * NNEG, np.int8)
+        self.h_labels = labels
+        self.lab = torch.from_numpy(labels).cuda()
+        self.w = torch.empty(n, dtype=torch.float32, device="cuda")
+        self.w0 = torch.from_numpy(np.where(labels > 0, np.float32(0.5) / np.float32(NPOS),
+                                            np.float32(0.5) / np.float32(NNEG)).astype(np.float32)).cuda()
+        self.strong = torch.zeros(n, dtype=torch.float32, device="cuda")
+        self.used = torch.zeros(len(pool), dtype=torch.uint8, device="cuda")
+        self.best = torch.zeros(4, dtype=torch.int32, device="cuda")
+        self.weaks = torch.zeros(ROUNDS * 7, dtype=torch.int32, device="cuda")
+        self.calib = torch.zeros(8, dtype=torch.int32, device="cuda")
+        self.t = V.AdaBoostTrainer((24, 24), n)
+        assert self.t.setFeaturePool(pool) == 0
+        self.ii = dict(nSamples=n, d_sumT=self.sumT, d_invNorm=self.inv)
+
+    def step(self, stream=None):
+        """One stage step: integrals, resident sort, ROUNDS rounds (no host sync)."""
+        V, torch = self.V, self.torch
+        V._capi.call("vj_integral_batch", self.d_p.data_ptr(), 24, 24, 24, self.n, self.sumT.data_ptr(), None,
+                     self.inv.data_ptr(), stream)
+        self.w.copy_(self.w0)
+        self.strong.zero_()
+        self.used.zero_()
+        assert self.t.bindTrainingSet(self.ii, self.lab, None, self.w) == 0
+        assert self.t.prepareStage(stream) == 0
+        for r in range(ROUNDS):
+            assert self.t.bestWeak(self.used, self.best, stream) == 0
+            wk = self.weaks[r * 7:(r + 1) * 7]
+            assert self.t.applyBestWeak(self.best, self.strong, self.used, wk, stream) == 0
+            assert self.t.calibrateStage(self.strong, self.numPos, 0.99, 0.4, NNEG, self.calib, stream) == 0
+
+
+def profile_read(V, reset=True):
+    import ctypes as C
+    lib = V.load()
+    n = C.c_int()
+    lib.vj_profile_read(None, 0, C.byref(n), 0)
+    buf = (C.c_char * (64 * max(1, n.value)))()
+    lib.vj_profile_read(C.addressof(buf), n.value, C.byref(n), int(reset))
+    out = {}
+    raw = bytes(buf)
+    for i in range(n.value):
+        rec = raw[i * 64:(i + 1) * 64]
+        name = rec[:48].split(b"\0")[0].decode()
+        launches = int.from_bytes(rec[48:56], "little", signed=True)
+        ms = float(np.frombuffer(rec[56:64], dtype=np.float64)[0])
+        out[name] = (launches, ms)
+    return out
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import cs677s26_gb300 as V
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    pool = V.feature_pool(V.FeatureMode.Basic)
+    F = len(pool)
+    patches = V.synth_patches(SEED, NPOS, NNEG)
+    n = len(patches)
+    st = Stage(torch, V, patches, pool)
+    # warm-up
+    for _ in range(args.warmup):
+        st.step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    V.load().vj_profile_enable(1)
+    profile_read(V, reset=True)
+    with Clocks(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0.record()
+        for _ in range(args.steps):
+            st.step()
+        t1.record()
+        torch.cuda.synchronize()
+    V.load().vj_profile_enable(0)
+    prof = profile_read(V, reset=True)
+    ms = t0.elapsed_time(t1)
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+        if dist:
+            dist.barrier()
+    ms_step = ms / args.steps
+    units = BYTES_PER_ELEM_ROUND * F * n * ROUNDS
+    value = world * units / (ms_step * 1e-3) / 1e9
+
+    # picks of the last step (sanity: deterministic across steps)
+    weaks = st.weaks.cpu().numpy().view(V.WEAK)
+
+    # ---- end to end through the C ABI with host buffers: upload the patches,
+    # train the step, read the 50 weak classifiers back.
+    h_p = torch.from_numpy(patches).pin_memory()
+    h_w = torch.empty(ROUNDS * 7, dtype=torch.int32).pin_memory()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(e2e_steps):
+        st.d_p.copy_(h_p, non_blocking=True)
+        st.step()
+        h_w.copy_(st.weaks, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / e2e_steps
+    if dist:
+        tt = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_e2e = float(tt.item())
+    e2e_value = world * units / (ms_e2e * 1e-3) / 1e9
+
+    # ---- roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 1.0))
+    name, (launches, total) = dom
+    ord_stride = (n + 7) & ~7
+    gap_stride = (n + 31) // 32
+    kbytes = {
+        # resident sweep: sorted order (2 B) + split bitmask (1/8 B) per feature-sample
+        "sweep_kernel": F * (ord_stride * 2 + gap_stride * 4),
+        # eval+sort: reads the L2-resident integrals, writes order + bitmask
+        "eval_sort_kernel": F * (ord_stride * 2 + gap_stride * 4) + 625 * n * 4,
+    }.get(name)
+    avg_ms = total / max(1, launches)
+    roof = {"kernel": name, "bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
+            "avg_launch_ms": avg_ms, "launches": launches, "share_of_step": total / ms if ms else None,
+            "traffic": None}
+    if kbytes:
+        ach = kbytes / (avg_ms * 1e-3) / 1e9
+        roof.update({"achieved": ach, "frac": ach / peak, "algorithmic_bytes_per_launch": kbytes})
+    gpu_launches = sum(v[0] for v in prof.values())
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (int32 responses, FP64 renorm)", "data": "synthetic",
+        "config": {"workload": "full stage training step (BASELINE configs[1]): 10,000+10,000 24x24 patches "
+                               "(seed 1), 162,336 Basic features, 50 boosting rounds",
+                   "features": F, "samples": n, "rounds": ROUNDS, "parallelism": f"replicas x{world}",
+                   "l2": "per-round working set (sorted orders 6.9 GB) exceeds L2"},
+        "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": int(patches.nbytes),
+                "d2h_bytes_per_step": int(ROUNDS * 28)},
+        "gpu_launches": gpu_launches, "roofline": roof,
+        "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in sorted(prof.items())},
+        "ms_per_round": ms_step / ROUNDS,
+        "clocks": clk.summary(),
+        "picks_head": [int(x) for x in weaks["featureIdx"][:5]],
+    }
+    if rank == 0:
+        result["cpu_baseline"] = cpu_baseline(pool, patches)
+    if dist:
+        dist.destroy_process_group()
+    return result
+
+
+# ----------------------------------------------------------------------------- CPU (oracle) arm
+def cpu_sample(pool, patches, nfeat, threads):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    feats = np.ascontiguousarray(pool[:nfeat]).view(O.FEATURE)
+    labels = np.array([1] * NPOS + [-1] * NNEG, np.int8)
+    w = np.where(labels > 0, np.float32(0.5) / np.float32(NPOS), np.float32(0.5) / np.float32(NNEG)).astype(np.float32)
+    sums, inv = O.train_integrals(patches)
+    t = time.perf_counter()
+    O.weak_search(feats, sums, inv, labels, w, threads=threads)
+    return time.perf_counter() - t
+
+
+def cpu_baseline(pool, patches, target_s=15.0):
+    threads = os.cpu_count() or 1
+    n = len(patches)
+    nfeat = 64 * threads
+    dt = cpu_sample(pool, patches, nfeat, threads)
+    nfeat = int(min(len(pool), max(nfeat, nfeat * target_s / max(dt, 1e-3))))
+    dt = cpu_sample(pool, patches, nfeat, threads)
+    gbs = BYTES_PER_ELEM_ROUND * nfeat * n / dt / 1e9
+    return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"one round of the oracle's restatement of runCpuWeakSearch over {nfeat} of 162,336 "
+                      f"features x {n} samples ({dt:.1f} s, {threads} threads), scaled by the 20 B model"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import cs677s26_gb300 as V
+    pool = V.feature_pool(V.FeatureMode.Basic)
+    patches = V.synth_patches(SEED, NPOS, NNEG)
+    threads = os.cpu_count() or 1
+    n = len(patches)
+    nfeat = 32 * threads
+    for _ in range(args.warmup):
+        cpu_sample(pool, patches, max(threads, nfeat // 4), threads)
+    times = [cpu_sample(pool, patches, nfeat, threads) for _ in range(args.steps)]
+    dt = sum(times) / len(times)
+    value = BYTES_PER_ELEM_ROUND * nfeat * n / dt / 1e9
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "full stage training step (BASELINE configs[1]): 10,000+10,000 24x24 patches "
+                               "(seed 1), 162,336 Basic features; each step is one round over a feature sample",
+                   "features_per_step": nfeat, "samples": n},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"{nfeat} features x {n} samples per step (oracle restatement of "
+                                   "runCpuWeakSearch; the reference binary cannot be built on this machine)"},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_gpu(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,68 @@
+// Device helpers shared by the kernels of libvjgb.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "common.h"
+#include "profiler.h"
+
+namespace vjgb {
+
+#define VJ_CUDA_TRY(expr)                                                              \
+    do {                                                                               \
+        cudaError_t e_ = (expr);                                                       \
+        if (e_ != cudaSuccess)                                                         \
+            return ::vjgb::set_error(e_ == cudaErrorMemoryAllocation ? VJ_OUT_OF_MEMORY \
+                                                                     : VJ_CUDA_ERROR,  \
+                                     std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define VJ_LAUNCH_CHECK(what)                                                         \
+    do {                                                                              \
+        cudaError_t e_ = cudaGetLastError();                                          \
+        if (e_ != cudaSuccess)                                                        \
+            return ::vjgb::set_error(VJ_CUDA_ERROR,                                   \
+                                     std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Radix key of a float: unsigned order equals float order, -0.0 before +0.0
+// (the order of a float radix sort).
+__device__ __forceinline__ uint32_t radix_key(uint32_t bits) {
+    return bits ^ (static_cast<uint32_t>(static_cast<int32_t>(bits) >> 31) | 0x80000000u);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Integral-image corner as the reference reads it: the int32 value converted
+// to float with round-to-nearest (face_vision_engine.cu:474, main.cu:485-487).
+__device__ __forceinline__ float corner_f(uint32_t v) { return __int2float_rn(static_cast<int32_t>(v)); }
+
+// Training response of one feature on sample s from the transposed sums
+// [625][n]: per rectangle (c0 - c1 - c2 + c3) in float, left to right, then
+// w0*s0 + w1*s1 (+ w2*s2), times invNorm, each operation rounded on its own
+// (main.cu:476-496, boosting_core.cu:249-260).
+__device__ __forceinline__ float train_response(const vj_haar_feature& f, const uint32_t* __restrict__ sumT,
+                                                int n, int s, float invNorm) {
+    const size_t N = static_cast<size_t>(n);
+    auto rs = [&](const vj_fast_rect& r) {
+        const float a = corner_f(__ldg(sumT + static_cast<size_t>(r.p0) * N + s));
+        const float b = corner_f(__ldg(sumT + static_cast<size_t>(r.p1) * N + s));
+        const float c = corner_f(__ldg(sumT + static_cast<size_t>(r.p2) * N + s));
+        const float d = corner_f(__ldg(sumT + static_cast<size_t>(r.p3) * N + s));
+        return __fadd_rn(__fsub_rn(__fsub_rn(a, b), c), d);
+    };
+    const float s0 = rs(f.r0);
+    const float s1 = rs(f.r1);
+    float resp = __fadd_rn(__fmul_rn(f.r0.w, s0), __fmul_rn(f.r1.w, s1));
+    if (f.rectCount == 3) resp = __fadd_rn(resp, __fmul_rn(f.r2.w, rs(f.r2)));
+    return __fmul_rn(resp, invNorm);
+}
+
+inline int div_up(int64_t a, int64_t b) { return static_cast<int>((a + b - 1) / b); }
+
+}  // namespace vjgb

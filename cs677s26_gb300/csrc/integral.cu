@@ -1,0 +1,397 @@
+// Integral and squared-integral images on sm_103a.
+//
+// Reference: RowPrefixKernel + ColumnScanTransposeKernel /
+// ColumnScanTransposeSingleSampleKernel + ComputeInvNormKernel
+// (src/face_vision_engine.cu:47-259, driver :1057-1158).  The reference keeps
+// int32 sums and int32 squared sums (wrapping mod 2^32); here sums are uint32
+// (the same bits) and squared sums are exact uint64 whose low 32 bits are the
+// reference's bits.
+//
+// Training batches (24x24 patches, transposed [625][n] layout): one thread
+// per sample keeps its running column sums in registers and writes each
+// integral pixel for 32 consecutive samples per warp store, so every store is
+// a full 128-byte (sum) / 256-byte (squared sum) line.
+//
+// Detection levels (row-major): a row pass (one warp per row, 16 pixels per
+// lane, warp shuffle scan, 16-byte stores of exclusive prefixes), then two
+// column passes over 32-column x 32-row segments: segment totals, then the
+// in-place column scan with the carry of the segments above.  All levels of
+// all images of a batch go through one launch of each pass.
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "integral.cuh"
+
+namespace vjgb {
+namespace {
+
+// invNorm of face_vision_engine.cu:216-259: over the interior
+// (1, 1, iiW-3, iiH-3), each corner read as the reference's int32 value and
+// converted to double, nf2 = area*sq - s*s, 1/sqrt(nf2) rounded to float.
+__device__ __forceinline__ float inv_norm(uint32_t s0, uint32_t s1, uint32_t s2, uint32_t s3, uint64_t q0,
+                                          uint64_t q1, uint64_t q2, uint64_t q3, int iiW, int iiH) {
+    if (iiW < 3 || iiH < 3) return 1.0f;
+    const double area = static_cast<double>((iiW - 3) * (iiH - 3));
+    auto i2d = [](uint32_t v) { return static_cast<double>(static_cast<int32_t>(v)); };
+    auto q2d = [](uint64_t v) { return static_cast<double>(static_cast<int32_t>(static_cast<uint32_t>(v))); };
+    const double s = i2d(s0) - i2d(s1) - i2d(s2) + i2d(s3);
+    const double q = q2d(q0) - q2d(q1) - q2d(q2) + q2d(q3);
+    const double nf2 = area * q - s * s;
+    return nf2 > 1e-12 ? static_cast<float>(1.0 / sqrt(nf2)) : 0.0f;
+}
+
+// 24x24 training patches, one thread per sample.
+__global__ void __launch_bounds__(128)
+train_integral24_kernel(const uint8_t* __restrict__ gray, int stride, int n, uint32_t* __restrict__ sumT,
+                        uint64_t* __restrict__ sqT, float* __restrict__ invNorm) {
+    constexpr int W = 24, IIW = 25;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const size_t N = static_cast<size_t>(n);
+    const uint8_t* img = gray + static_cast<size_t>(s) * W * stride;
+    uint32_t cs[W];
+    uint64_t cq[W];
+#pragma unroll
+    for (int x = 0; x < W; ++x) {
+        cs[x] = 0;
+        cq[x] = 0;
+    }
+#pragma unroll
+    for (int c = 0; c < IIW; ++c) {
+        sumT[c * N + s] = 0;
+        if (sqT) sqT[c * N + s] = 0;
+    }
+    uint32_t k11 = 0, k23 = 0, k1y = 0, k2y = 0;
+    uint64_t q11 = 0, q23 = 0, q1y = 0, q2y = 0;
+    for (int y = 1; y <= W; ++y) {
+        const uint8_t* prow = img + static_cast<size_t>(y - 1) * stride;
+        uint8_t px[W];
+#pragma unroll
+        for (int x = 0; x < W; ++x) px[x] = __ldg(prow + x);
+        const size_t rb = static_cast<size_t>(y) * IIW;
+        sumT[rb * N + s] = 0;
+        if (sqT) sqT[rb * N + s] = 0;
+        uint32_t rs = 0, rq = 0;
+#pragma unroll
+        for (int x = 0; x < W; ++x) {
+            rs += px[x];
+            rq += static_cast<uint32_t>(px[x]) * px[x];
+            cs[x] += rs;
+            cq[x] += rq;
+            sumT[(rb + x + 1) * N + s] = cs[x];
+            if (sqT) sqT[(rb + x + 1) * N + s] = cq[x];
+        }
+        if (y == 1) {
+            k11 = cs[0];
+            k23 = cs[22];
+            q11 = cq[0];
+            q23 = cq[22];
+        }
+        if (y == 23) {
+            k1y = cs[0];
+            k2y = cs[22];
+            q1y = cq[0];
+            q2y = cq[22];
+        }
+    }
+    if (invNorm) invNorm[s] = inv_norm(k11, k23, k1y, k2y, q11, q23, q1y, q2y, IIW, IIW);
+}
+
+// Any patch size: same arithmetic, previous integral row read back.
+__global__ void __launch_bounds__(128)
+train_integral_generic_kernel(const uint8_t* __restrict__ gray, int w, int h, int stride, int n,
+                              uint32_t* __restrict__ sumT, uint64_t* __restrict__ sqT, float* __restrict__ invNorm) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const size_t N = static_cast<size_t>(n);
+    const int iiW = w + 1, iiH = h + 1;
+    const uint8_t* img = gray + static_cast<size_t>(s) * h * stride;
+    for (int c = 0; c < iiW; ++c) {
+        sumT[c * N + s] = 0;
+        if (sqT) sqT[c * N + s] = 0;
+    }
+    for (int y = 1; y <= h; ++y) {
+        const uint8_t* prow = img + static_cast<size_t>(y - 1) * stride;
+        const size_t rb = static_cast<size_t>(y) * iiW;
+        sumT[rb * N + s] = 0;
+        if (sqT) sqT[rb * N + s] = 0;
+        uint32_t rs = 0;
+        uint64_t rq = 0;
+        for (int x = 1; x <= w; ++x) {
+            const uint32_t p = prow[x - 1];
+            rs += p;
+            rq += p * p;
+            const size_t i = rb + x;
+            sumT[i * N + s] = sumT[(i - iiW) * N + s] + rs;
+            if (sqT) sqT[i * N + s] = sqT[(i - iiW) * N + s] + rq;
+        }
+    }
+    if (invNorm) {
+        if (iiW < 3 || iiH < 3 || !sqT) {
+            invNorm[s] = 1.0f;
+            return;
+        }
+        const int ww = iiW - 3, hh = iiH - 3;
+        const size_t p0 = 1 + iiW, p1 = (1 + ww) + iiW, p2 = 1 + static_cast<size_t>(iiW) * (1 + hh),
+                     p3 = (1 + ww) + static_cast<size_t>(iiW) * (1 + hh);
+        invNorm[s] = inv_norm(sumT[p0 * N + s], sumT[p1 * N + s], sumT[p2 * N + s], sumT[p3 * N + s],
+                              sqT[p0 * N + s], sqT[p1 * N + s], sqT[p2 * N + s], sqT[p3 * N + s], iiW, iiH);
+    }
+}
+
+__device__ __forceinline__ int find_job(const IIJob* __restrict__ jobs, int njobs, int64_t item, bool byRow) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int64_t b = byRow ? jobs[mid].rowBase : jobs[mid].itemBase;
+        if (b <= item)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Row pass: integral row 0 is zero; row y >= 1 holds, at column c, the sum of
+// pixels [0, c) of image row y-1 (and the sum of their squares).
+__global__ void __launch_bounds__(256)
+row_pass_kernel(const IIJob* __restrict__ jobs, int njobs, int64_t rows) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t r = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < rows; r += nw) {
+        const IIJob J = jobs[find_job(jobs, njobs, r, true)];
+        const int y = static_cast<int>(r - J.rowBase);
+        uint32_t* srow = J.sum + static_cast<size_t>(y) * J.pitch;
+        uint64_t* qrow = J.sq + static_cast<size_t>(y) * J.pitch;
+        const bool vecOut = ((J.pitch & 3) == 0) && ((reinterpret_cast<uintptr_t>(J.sum) & 15) == 0) &&
+                            ((reinterpret_cast<uintptr_t>(J.sq) & 15) == 0);
+        const uint8_t* prow = y > 0 ? J.pix + static_cast<size_t>(y - 1) * J.stride : nullptr;
+        uint32_t carryS = 0, carryQ = 0;
+        for (int cb = 0; cb <= J.w; cb += 512) {
+            const int c0 = cb + lane * 16;
+            uint32_t p[16];
+            if (y == 0) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) p[i] = 0;
+            } else if (c0 + 16 <= J.w && ((reinterpret_cast<uintptr_t>(prow + c0) & 15) == 0)) {
+                const uint4 v = __ldg(reinterpret_cast<const uint4*>(prow + c0));
+                const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int i = 0; i < 16; ++i) p[i] = (wv[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) p[i] = (c0 + i < J.w) ? __ldg(prow + c0 + i) : 0u;
+            }
+            uint32_t es[16], eq[16];
+            uint32_t ls = 0, lq = 0;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                es[i] = ls;
+                eq[i] = lq;
+                ls += p[i];
+                lq += p[i] * p[i];
+            }
+            uint32_t is = ls, iq = lq;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t ys = __shfl_up_sync(0xffffffffu, is, o);
+                const uint32_t yq = __shfl_up_sync(0xffffffffu, iq, o);
+                if (lane >= o) {
+                    is += ys;
+                    iq += yq;
+                }
+            }
+            const uint32_t bs = carryS + is - ls, bq = carryQ + iq - lq;
+            carryS += __shfl_sync(0xffffffffu, is, 31);
+            carryQ += __shfl_sync(0xffffffffu, iq, 31);
+            if (vecOut && c0 + 15 <= J.w) {
+                uint4* so = reinterpret_cast<uint4*>(srow + c0);
+                ulonglong2* qo = reinterpret_cast<ulonglong2*>(qrow + c0);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    so[i] = make_uint4(bs + es[4 * i], bs + es[4 * i + 1], bs + es[4 * i + 2], bs + es[4 * i + 3]);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    qo[i] = make_ulonglong2(static_cast<uint64_t>(bq + eq[2 * i]),
+                                            static_cast<uint64_t>(bq + eq[2 * i + 1]));
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    if (c0 + i <= J.w) {
+                        srow[c0 + i] = bs + es[i];
+                        qrow[c0 + i] = static_cast<uint64_t>(bq + eq[i]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void col_item(const IIJob& J, int64_t local, int lane, int* seg, int* c, int* r0, int* r1) {
+    const int chunks = (J.w + 1 + 31) >> 5;
+    *seg = static_cast<int>(local / chunks);
+    *c = static_cast<int>(local % chunks) * 32 + lane;
+    *r0 = 1 + *seg * kColSeg;
+    *r1 = min(J.h, (*seg + 1) * kColSeg);
+}
+
+// Column pass A: per 32-row segment and column, the sum of the row prefixes.
+__global__ void __launch_bounds__(256)
+col_total_kernel(const IIJob* __restrict__ jobs, int njobs, int64_t items, int64_t totPitch,
+                 uint32_t* __restrict__ totS, uint64_t* __restrict__ totQ) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t it = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; it < items; it += nw) {
+        const IIJob J = jobs[find_job(jobs, njobs, it, false)];
+        int seg, c, r0, r1;
+        col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
+        if (c > J.w) continue;
+        uint32_t s = 0;
+        uint64_t q = 0;
+        for (int r = r0; r <= r1; ++r) {
+            s += __ldg(J.sum + static_cast<size_t>(r) * J.pitch + c);
+            q += __ldg(J.sq + static_cast<size_t>(r) * J.pitch + c);
+        }
+        const size_t o = static_cast<size_t>(J.totBase + seg) * totPitch + c;
+        totS[o] = s;
+        totQ[o] = q;
+    }
+}
+
+// Column pass B: carry of the segments above, then the running column sum
+// written in place.
+__global__ void __launch_bounds__(256)
+col_scan_kernel(const IIJob* __restrict__ jobs, int njobs, int64_t items, int64_t totPitch,
+                const uint32_t* __restrict__ totS, const uint64_t* __restrict__ totQ) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t it = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; it < items; it += nw) {
+        const IIJob J = jobs[find_job(jobs, njobs, it, false)];
+        int seg, c, r0, r1;
+        col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
+        if (c > J.w) continue;
+        uint32_t s = 0;
+        uint64_t q = 0;
+        for (int k = 0; k < seg; ++k) {
+            const size_t o = static_cast<size_t>(J.totBase + k) * totPitch + c;
+            s += totS[o];
+            q += totQ[o];
+        }
+        for (int r = r0; r <= r1; ++r) {
+            const size_t o = static_cast<size_t>(r) * J.pitch + c;
+            s += J.sum[o];
+            q += J.sq[o];
+            J.sum[o] = s;
+            J.sq[o] = q;
+        }
+    }
+}
+
+int grid_for(int64_t warps) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t blocks = (warps + 7) / 8;
+    const int64_t cap = static_cast<int64_t>(sms > 0 ? sms : 1) * 16;
+    return static_cast<int>(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+}
+
+}  // namespace
+
+IIPlan plan_integral_jobs(IIJob* jobs, int njobs) {
+    IIPlan p{0, 0, 0, 0};
+    for (int i = 0; i < njobs; ++i) {
+        IIJob& J = jobs[i];
+        J.rowBase = p.rows;
+        J.itemBase = p.items;
+        J.totBase = p.totRows;
+        p.rows += J.h + 1;
+        p.items += static_cast<int64_t>(col_chunks(J.w)) * col_segs(J.h);
+        p.totRows += col_segs(J.h);
+        const int64_t cols = static_cast<int64_t>(col_chunks(J.w)) * 32;
+        if (cols > p.totPitch) p.totPitch = cols;
+    }
+    return p;
+}
+
+int launch_integral_jobs(const IIJob* d_jobs, int njobs, const IIPlan& plan, uint32_t* d_totS, uint64_t* d_totQ,
+                         cudaStream_t stream) {
+    if (njobs <= 0) return VJ_OK;
+    VJ_TIMED_LAUNCH("row_pass_kernel", stream,
+                    row_pass_kernel<<<grid_for(plan.rows), 256, 0, stream>>>(d_jobs, njobs, plan.rows));
+    VJ_LAUNCH_CHECK("row_pass_kernel");
+    VJ_TIMED_LAUNCH("col_total_kernel", stream,
+                    col_total_kernel<<<grid_for(plan.items), 256, 0, stream>>>(d_jobs, njobs, plan.items,
+                                                                               plan.totPitch, d_totS, d_totQ));
+    VJ_LAUNCH_CHECK("col_total_kernel");
+    VJ_TIMED_LAUNCH("col_scan_kernel", stream,
+                    col_scan_kernel<<<grid_for(plan.items), 256, 0, stream>>>(d_jobs, njobs, plan.items,
+                                                                              plan.totPitch, d_totS, d_totQ));
+    VJ_LAUNCH_CHECK("col_scan_kernel");
+    return VJ_OK;
+}
+
+}  // namespace vjgb
+
+using namespace vjgb;
+
+extern "C" {
+
+int vj_integral_batch(const uint8_t* d_gray, int w, int h, int stride, int n, uint32_t* d_sumT,
+                      uint64_t* d_sqsumT, float* d_invNorm, void* stream) {
+    if (!d_gray || !d_sumT || w <= 0 || h <= 0 || stride < w || n <= 0)
+        return set_error(VJ_INVALID_ARG, "vj_integral_batch: bad arguments");
+    if (static_cast<int64_t>(w) * h * 255 >= (1LL << 31))
+        return set_error(VJ_INVALID_ARG, "vj_integral_batch: image too large for 32-bit sums");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int grid = div_up(n, 128);
+    if (w == 24 && h == 24) {
+        VJ_TIMED_LAUNCH("train_integral24_kernel", s,
+                        train_integral24_kernel<<<grid, 128, 0, s>>>(d_gray, stride, n, d_sumT, d_sqsumT, d_invNorm));
+    } else {
+        if (d_invNorm && !d_sqsumT)
+            return set_error(VJ_INVALID_ARG, "vj_integral_batch: invNorm needs the squared sums for this size");
+        VJ_TIMED_LAUNCH("train_integral_generic_kernel", s,
+                        train_integral_generic_kernel<<<grid, 128, 0, s>>>(d_gray, w, h, stride, n, d_sumT, d_sqsumT,
+                                                                           d_invNorm));
+    }
+    VJ_LAUNCH_CHECK("train_integral_kernel");
+    return ok();
+}
+
+int vj_integral_image(const uint8_t* d_gray, int w, int h, int stride, uint32_t* d_sum, uint64_t* d_sqsum,
+                      void* stream) {
+    if (!d_gray || !d_sum || w <= 0 || h <= 0 || stride < w || w > 65535 || h > 65535)
+        return set_error(VJ_INVALID_ARG, "vj_integral_image: bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    IIJob job{};
+    job.pix = d_gray;
+    job.stride = stride;
+    job.sum = d_sum;
+    job.w = w;
+    job.h = h;
+    job.pitch = w + 1;
+    uint64_t* sq = d_sqsum;
+    if (!sq) VJ_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&sq), sizeof(uint64_t) * (w + 1) * (h + 1), s));
+    job.sq = sq;
+    IIPlan plan = plan_integral_jobs(&job, 1);
+    IIJob* d_job = nullptr;
+    uint32_t* totS = nullptr;
+    uint64_t* totQ = nullptr;
+    VJ_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_job), sizeof(IIJob), s));
+    VJ_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&totS), sizeof(uint32_t) * plan.totRows * plan.totPitch, s));
+    VJ_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&totQ), sizeof(uint64_t) * plan.totRows * plan.totPitch, s));
+    VJ_CUDA_TRY(cudaMemcpyAsync(d_job, &job, sizeof(IIJob), cudaMemcpyHostToDevice, s));
+    const int st = launch_integral_jobs(d_job, 1, plan, totS, totQ, s);
+    cudaFreeAsync(d_job, s);
+    cudaFreeAsync(totS, s);
+    cudaFreeAsync(totQ, s);
+    if (!d_sqsum) cudaFreeAsync(sq, s);
+    if (st != VJ_OK) return st;
+    // The job descriptor lives on the host stack: finish the copy before returning.
+    VJ_CUDA_TRY(cudaStreamSynchronize(s));
+    return ok();
+}
+
+}  // extern "C"

@@ -1,0 +1,1199 @@
+// AdaBoost best-weak (decision stump) search and round update on sm_103a.
+//
+// Reference path (hengyizhu/CS677s26): per round, a tile loop of
+// EvaluateFeatureResponsesKernel -> cub::DeviceSegmentedRadixSort ->
+// EvaluateAndFindThresholdKernel -> SelectBestInTileKernel
+// (src/boosting_core.cu:221-456, src/main.cu:2013-2053), then
+// ReduceTileBestCandidatesKernel and the update kernels (main.cu:829-1028).
+// Its CPU twin runCpuWeakSearch (main.cu:587-682) defines the pick this file
+// reproduces bit for bit.
+//
+// Design here:
+//   1. eval_sort_kernel: one CTA per feature evaluates the exact normalised
+//      responses of all samples into shared memory and sorts them with an
+//      on-chip stable LSD radix sort (4 x 8-bit digits, warp match-any ranking,
+//      per-warp digit counters).  It writes the sorted sample order (2 B per
+//      feature-sample) and a bitmask of valid split positions
+//      (v[k] + 1e-7f < v[k+1], boosting_core.cu:400).
+//   2. sweep_kernel: one warp per feature streams that order, gathers signed
+//      weights from shared memory and forms FP32 prefix sums (8-element lane
+//      runs, warp shuffle scan, Kahan-compensated carries across chunks) to
+//      get each feature's minimum weighted error to within a proven bound.
+//   3. Candidates: every feature whose error is within 2*(bound of the
+//      reference's sequential FP32 arithmetic + bound of step 2) of the
+//      minimum.  The reference's pick is provably among them.
+//   4. refine_kernel: one thread per candidate replays the reference's
+//      sequential FP32 totals and sweep exactly (main.cu:626-678); the
+//      winner is the smallest FP32 error, ties to the lower featureIdx.
+// With vj_trainer_prepare_stage the orders of step 1 stay resident in HBM for
+// all rounds of a stage (the responses do not change within a stage, only
+// the weights), so a round costs steps 2-4 only.
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "device_util.cuh"
+
+namespace vjgb {
+namespace {
+
+constexpr int kSortThreads = 1024;
+constexpr int kCntStride = 33;  // per-digit row of 32 warp counters, padded against bank conflicts
+constexpr int kSweepThreads = 512;
+constexpr int kSweepWarps = kSweepThreads / 32;
+constexpr int kSmemWeightsMax = 49152;  // samples whose weights fit in shared memory
+constexpr float kU = 5.9604645e-08f;    // 2^-24, unit roundoff of FP32
+
+struct RoundParams {
+    float tp, tn, w;             // active positive / negative weight and their sum
+    float window;                // candidate window above the fast minimum
+    unsigned int fastMinBits;    // min fast error over features (float bits, >= 0)
+    int ncand;                   // number of candidates
+    unsigned long long winner;   // (FP32 error bits << 32) | featureIdx; min wins
+    int np, nn;                  // active positive / negative sample counts
+    int status;                  // 0 ok, 1 no valid split anywhere
+};
+
+// ---------------------------------------------------------------------------
+// 1. Evaluate + on-chip stable radix sort of one feature per CTA.
+// ---------------------------------------------------------------------------
+template <int R>
+constexpr size_t sort_smem_bytes() {
+    return static_cast<size_t>(1024 * R) * (4 + 2) + 256 * kCntStride * 4;
+}
+
+template <int R, bool kFromResp>
+__global__ void __launch_bounds__(kSortThreads, 1)
+eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int featCount,
+                 const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm, int n,
+                 const float* __restrict__ resp, uint16_t* __restrict__ ordOut, int64_t ordStride,
+                 bool ordPadded, uint32_t* __restrict__ gapOut, int64_t gapStride) {
+    constexpr int NP = 1024 * R;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);  // float bits in sample order
+    uint16_t* idx = reinterpret_cast<uint16_t*>(keys + NP);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(idx + NP);
+    __shared__ uint32_t warpTot[32];
+    __shared__ vj_haar_feature sfeat;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gapWords = (n + 31) >> 5;
+
+    for (int fl = blockIdx.x; fl < featCount; fl += gridDim.x) {
+        if (kFromResp) {
+            const float* row = resp + static_cast<size_t>(fl) * n;
+            for (int s = tid; s < n; s += kSortThreads) keys[s] = __float_as_uint(row[s]);
+        } else {
+            if (tid == 0) sfeat = feats[featBegin + fl];
+            __syncthreads();
+            const vj_haar_feature f = sfeat;
+            for (int s = tid; s < n; s += kSortThreads)
+                keys[s] = __float_as_uint(train_response(f, sumT, n, s, __ldg(invNorm + s)));
+        }
+        for (int p = tid; p < NP; p += kSortThreads) idx[p] = static_cast<uint16_t>(p);
+        __syncthreads();
+
+        for (int pass = 0; pass < 4; ++pass) {
+            const int shift = pass * 8;
+            for (int i = tid; i < 256 * kCntStride; i += kSortThreads) cnt[i] = 0;
+            __syncthreads();
+            // Rank every item among equal digits: items are warp-striped, so
+            // (warp, j, lane) order is the current sequence order and ranks are
+            // stable.  The leader of each equal-digit group bumps the warp's
+            // counter for that digit.
+            uint32_t packed[R];
+            uint32_t dig[(R + 3) / 4];
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                const int p = warp * 32 * R + j * 32 + lane;
+                const uint32_t id = idx[p];
+                const uint32_t d = id < static_cast<uint32_t>(n) ? (radix_key(keys[id]) >> shift) & 255u : 255u;
+                const uint32_t peers = __match_any_sync(0xffffffffu, d);
+                const int leader = __ffs(peers) - 1;
+                uint32_t old = 0;
+                if (lane == leader) {
+                    old = cnt[d * kCntStride + warp];
+                    cnt[d * kCntStride + warp] = old + __popc(peers);
+                }
+                old = __shfl_sync(0xffffffffu, old, leader);
+                packed[j] = id | ((old + __popc(peers & lanemask_lt())) << 16);
+                if ((j & 3) == 0)
+                    dig[j >> 2] = d;
+                else
+                    dig[j >> 2] |= d << (8 * (j & 3));
+            }
+            __syncthreads();
+            // Exclusive scan of the counters in (digit, warp) order.
+            {
+                const int d = tid >> 2, w0 = (tid & 3) * 8;
+                uint32_t v[8];
+                uint32_t run = 0;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const uint32_t t = cnt[d * kCntStride + w0 + i];
+                    v[i] = run;
+                    run += t;
+                }
+                uint32_t incl = run;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (lane == 31) warpTot[warp] = incl;
+                __syncthreads();
+                if (warp == 0) {
+                    const uint32_t t = warpTot[lane];
+                    uint32_t s = t;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                        if (lane >= o) s += y;
+                    }
+                    warpTot[lane] = s - t;
+                }
+                __syncthreads();
+                const uint32_t base = warpTot[warp] + incl - run;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) cnt[d * kCntStride + w0 + i] = base + v[i];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                const uint32_t d = (dig[j >> 2] >> (8 * (j & 3))) & 255u;
+                const uint32_t pos = cnt[d * kCntStride + warp] + (packed[j] >> 16);
+                idx[pos] = static_cast<uint16_t>(packed[j] & 0xFFFFu);
+            }
+            __syncthreads();
+        }
+
+        // Sorted sample order.
+        uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
+        if (ordPadded) {
+            const int n8 = (n + 7) & ~7;
+            for (int k = tid * 8; k < n8; k += kSortThreads * 8)
+                *reinterpret_cast<uint4*>(orow + k) = *reinterpret_cast<const uint4*>(idx + k);
+        } else {
+            for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
+        }
+        // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
+        if (gapOut) {
+            uint32_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
+            for (int wd = tid; wd < gapWords; wd += kSortThreads) {
+                uint32_t bits = 0;
+                const int k0 = wd * 32;
+                float v0 = __uint_as_float(keys[idx[k0]]);
+                for (int b = 0; b < 32; ++b) {
+                    const int k = k0 + b;
+                    if (k + 1 >= n) break;
+                    const float v1 = __uint_as_float(keys[idx[k + 1]]);
+                    if (__fadd_rn(v0, 1e-7f) < v1) bits |= 1u << b;
+                    v0 = v1;
+                }
+                grow[wd] = bits;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-round weight preparation: signed weights (+w positive, -w negative,
+// +-0 inactive), totals and the candidate window.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024)
+prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
+                  const float* __restrict__ weight, int n, float* __restrict__ wsg,
+                  RoundParams* __restrict__ prm) {
+    __shared__ double sp[32], sn[32];
+    __shared__ int cp[32], cn[32];
+    double tp = 0.0, tn = 0.0;
+    int np = 0, nn = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const bool act = active == nullptr || active[i] != 0;
+        const float w = act ? weight[i] : 0.0f;
+        const bool pos = label[i] > 0;
+        wsg[i] = pos ? w : -w;
+        if (act) {
+            if (pos) {
+                tp += static_cast<double>(w);
+                ++np;
+            } else {
+                tn += static_cast<double>(w);
+                ++nn;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        tp += __shfl_down_sync(0xffffffffu, tp, o);
+        tn += __shfl_down_sync(0xffffffffu, tn, o);
+        np += __shfl_down_sync(0xffffffffu, np, o);
+        nn += __shfl_down_sync(0xffffffffu, nn, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        sp[warp] = tp;
+        sn[warp] = tn;
+        cp[warp] = np;
+        cn[warp] = nn;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double TP = 0.0, TN = 0.0;
+        int NP = 0, NN = 0;
+        for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) {
+            TP += sp[k];
+            TN += sn[k];
+            NP += cp[k];
+            NN += cn[k];
+        }
+        const double u = 5.9604644775390625e-08;
+        auto gamma = [&](int k) { return static_cast<double>(k) * u / (1.0 - static_cast<double>(k) * u); };
+        const double W = TP + TN;
+        // |sequential FP32 error - exact| for either parity (see the header).
+        const double bcpu = 2.0 * gamma(NP + 2) * TP + 2.0 * gamma(NN + 2) * TN + 4.0 * u * W;
+        const double bfast = 64.0 * u * W;
+        const double window = 2.0 * (bcpu + bfast) * 1.01 + 1e-30;
+        prm->tp = static_cast<float>(TP);
+        prm->tn = static_cast<float>(TN);
+        prm->w = static_cast<float>(W);
+        prm->window = static_cast<float>(window);
+        prm->fastMinBits = 0x7F800000u;
+        prm->ncand = 0;
+        prm->winner = ~0ull;
+        prm->np = NP;
+        prm->nn = NN;
+        prm->status = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2. Fast sweep: one warp per feature, minimum weighted error to within the
+//    bound used for the window.
+// ---------------------------------------------------------------------------
+template <bool kSmemW>
+__global__ void __launch_bounds__(kSweepThreads, 2)
+sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
+             int64_t gapStride, const float* __restrict__ wsgG, int n, int featCount,
+             const uint8_t* __restrict__ usedMask, RoundParams* __restrict__ prm,
+             float* __restrict__ fastErr) {
+    extern __shared__ float wsgS[];
+    const float* wsg = wsgG;
+    if (kSmemW) {
+        for (int i = threadIdx.x; i < n; i += kSweepThreads) wsgS[i] = wsgG[i];
+        __syncthreads();
+        wsg = wsgS;
+    }
+    const float TP = prm->tp, W = prm->w;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float blockMin = INFINITY;
+    for (int f = blockIdx.x * kSweepWarps + warp; f < featCount; f += gridDim.x * kSweepWarps) {
+        float best = INFINITY;
+        if (!(usedMask && usedMask[f])) {
+            const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
+            const uint32_t* grow = gap + static_cast<size_t>(f) * gapStride;
+            float cp = 0.0f, cn = 0.0f, kp = 0.0f, kn = 0.0f;
+            for (int base = 0; base < n - 1; base += 256) {
+                const int k0 = base + lane * 8;
+                uint4 v = make_uint4(0, 0, 0, 0);
+                uint32_t g = 0;
+                if (k0 < n) v = __ldg(reinterpret_cast<const uint4*>(row + k0));
+                if (k0 < n - 1) g = (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu;
+                const uint32_t ids[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
+                                         v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+                float lp[8], ln[8];
+                float sp = 0.0f, sn = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    // positions past n hold padding indices: read sample 0, add nothing
+                    const bool in = k0 + i < n;
+                    const float x = in ? wsg[in ? ids[i] : 0u] : 0.0f;
+                    sp = __fadd_rn(sp, fmaxf(x, 0.0f));
+                    sn = __fadd_rn(sn, fmaxf(-x, 0.0f));
+                    lp[i] = sp;
+                    ln[i] = sn;
+                }
+                float ip = sp, in = sn;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float yp = __shfl_up_sync(0xffffffffu, ip, o);
+                    const float yn = __shfl_up_sync(0xffffffffu, in, o);
+                    if (lane >= o) {
+                        ip = __fadd_rn(ip, yp);
+                        in = __fadd_rn(in, yn);
+                    }
+                }
+                float ep = __shfl_up_sync(0xffffffffu, ip, 1);
+                float en = __shfl_up_sync(0xffffffffu, in, 1);
+                if (lane == 0) ep = en = 0.0f;
+                const float totp = __shfl_sync(0xffffffffu, ip, 31);
+                const float totn = __shfl_sync(0xffffffffu, in, 31);
+                const float bp = __fadd_rn(cp, ep), bn = __fadd_rn(cn, en);
+                if (g) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        if ((g >> i) & 1u) {
+                            const float Lp = __fadd_rn(bp, lp[i]);
+                            const float Ln = __fadd_rn(bn, ln[i]);
+                            const float eP = __fadd_rn(Ln, __fsub_rn(TP, Lp));
+                            const float eN = __fsub_rn(W, eP);
+                            best = fminf(best, fminf(eP, eN));
+                        }
+                    }
+                }
+                // Kahan-compensated carries across chunks.
+                {
+                    const float y = __fsub_rn(totp, kp);
+                    const float t = __fadd_rn(cp, y);
+                    kp = __fsub_rn(__fsub_rn(t, cp), y);
+                    cp = t;
+                }
+                {
+                    const float y = __fsub_rn(totn, kn);
+                    const float t = __fadd_rn(cn, y);
+                    kn = __fsub_rn(__fsub_rn(t, cn), y);
+                    cn = t;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_xor_sync(0xffffffffu, best, o));
+            best = fmaxf(best, 0.0f);
+        }
+        if (lane == 0) fastErr[f] = best;
+        blockMin = fminf(blockMin, best);
+    }
+    __shared__ float wmin[kSweepWarps];
+    if (lane == 0) wmin[warp] = blockMin;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = INFINITY;
+        for (int k = 0; k < kSweepWarps; ++k) m = fminf(m, wmin[k]);
+        if (m < INFINITY) atomicMin(&prm->fastMinBits, __float_as_uint(m));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. Candidate selection.
+// ---------------------------------------------------------------------------
+__global__ void select_candidates_kernel(const float* __restrict__ fastErr, int featCount,
+                                         RoundParams* __restrict__ prm, int* __restrict__ cand) {
+    const float lim = __fadd_rn(__uint_as_float(prm->fastMinBits), prm->window);
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < featCount; f += gridDim.x * blockDim.x) {
+        const float e = fastErr[f];
+        if (e <= lim && e < INFINITY) cand[atomicAdd(&prm->ncand, 1)] = f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. Exact replay of runCpuWeakSearch (main.cu:626-678) for each candidate:
+//    sequential FP32 totals over the sorted order, then the sequential sweep
+//    with the CPU's update rule (lower err wins; at equal err parity +1
+//    replaces parity -1).
+// ---------------------------------------------------------------------------
+template <bool kSmemW>
+__global__ void __launch_bounds__(256)
+refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
+              int64_t gapStride, const float* __restrict__ wsgG, int n, RoundParams* __restrict__ prm,
+              const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit) {
+    extern __shared__ float wsgS[];
+    const float* wsg = wsgG;
+    if (kSmemW) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) wsgS[i] = wsgG[i];
+        __syncthreads();
+        wsg = wsgS;
+    }
+    const int nc = prm->ncand;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int f = cand[c];
+        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
+        const uint32_t* grow = gap + static_cast<size_t>(f) * gapStride;
+        float tp = 0.0f, tn = 0.0f;
+        for (int k0 = 0; k0 < n; k0 += 8) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(row + k0));
+            const uint32_t ids[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
+                                     v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (k0 + i < n) {
+                    const float x = wsg[ids[i]];
+                    if (signbit(x))
+                        tn = __fadd_rn(tn, -x);
+                    else
+                        tp = __fadd_rn(tp, x);
+                }
+            }
+        }
+        float lp = 0.0f, ln = 0.0f, bestErr = INFINITY;
+        int bestPar = 1, bestK = -1;
+        for (int k0 = 0; k0 < n - 1; k0 += 8) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(row + k0));
+            const uint32_t ids[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
+                                     v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+            const uint32_t g = (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int k = k0 + i;
+                if (k < n - 1) {
+                    const float x = wsg[ids[i]];
+                    if (signbit(x))
+                        ln = __fadd_rn(ln, -x);
+                    else
+                        lp = __fadd_rn(lp, x);
+                    if ((g >> i) & 1u) {
+                        const float rp = __fsub_rn(tp, lp), rn = __fsub_rn(tn, ln);
+                        const float eL = __fadd_rn(ln, rp);
+                        if (eL < bestErr) {
+                            bestErr = eL;
+                            bestPar = -1;
+                            bestK = k;
+                        }
+                        const float eR = __fadd_rn(lp, rn);
+                        if (eR < bestErr || (eR == bestErr && bestPar < 1)) {
+                            bestErr = eR;
+                            bestPar = 1;
+                            bestK = k;
+                        }
+                    }
+                }
+            }
+        }
+        if (bestK >= 0) {
+            refParity[f] = static_cast<int8_t>(bestPar);
+            refSplit[f] = bestK;
+            const unsigned long long key =
+                (static_cast<unsigned long long>(__float_as_uint(bestErr)) << 32) | static_cast<unsigned>(f);
+            atomicMin(&prm->winner, key);
+        }
+    }
+}
+
+// 5. Winner -> TileBestCandidate with theta = 0.5f * (v[k] + v[k+1]).
+__global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const uint32_t* __restrict__ sumT,
+                                const float* __restrict__ invNorm, int n, const uint16_t* __restrict__ ord,
+                                int64_t ordStride, RoundParams* __restrict__ prm,
+                                const int8_t* __restrict__ refParity, const int* __restrict__ refSplit,
+                                vj_tile_best* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    vj_tile_best b;
+    b.pad0 = b.pad1 = b.pad2 = 0;
+    const unsigned long long w = prm->winner;
+    if (w == ~0ull) {
+        b.bestErr = INFINITY;
+        b.bestTheta = 0.0f;
+        b.featureIdx = -1;
+        b.bestParity = 1;
+        prm->status = 1;
+    } else {
+        const int f = static_cast<int>(w & 0xFFFFFFFFull);
+        const int k = refSplit[f];
+        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
+        const int s0 = row[k], s1 = row[k + 1];
+        const vj_haar_feature ft = feats[f];
+        const float v0 = train_response(ft, sumT, n, s0, invNorm[s0]);
+        const float v1 = train_response(ft, sumT, n, s1, invNorm[s1]);
+        b.bestErr = __uint_as_float(static_cast<uint32_t>(w >> 32));
+        b.bestTheta = __fmul_rn(0.5f, __fadd_rn(v0, v1));
+        b.featureIdx = f;
+        b.bestParity = refParity[f];
+    }
+    *out = b;
+}
+
+// ---------------------------------------------------------------------------
+// AdaBoost round update (main.cu:2082-2166, kernels main.cu:829-906) with FP64
+// alpha/log and renormalisation.  One CTA; each thread owns samples
+// t, t+1024, ... whose FP64 contributions it sums in that order; the 1024
+// partial sums are combined by a fixed halving tree, so the result does not
+// depend on scheduling.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024)
+round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_best* __restrict__ best,
+                    const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm,
+                    const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
+                    float* __restrict__ weight, float* __restrict__ strong, int n,
+                    uint8_t* __restrict__ usedMask, vj_weak_classifier* __restrict__ weakOut,
+                    int* __restrict__ status) {
+    __shared__ double part[1024];
+    __shared__ vj_haar_feature sfeat;
+    __shared__ float sTheta, sLeft, sRight;
+    __shared__ double sF;
+    __shared__ int sPar, sValid;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        const vj_tile_best b = *best;
+        const bool valid = b.featureIdx >= 0 && isfinite(b.bestErr);
+        sValid = valid ? 1 : 0;
+        if (valid) {
+            const float eps = 1e-6f;
+            const float e = fminf(fmaxf(b.bestErr, eps), __fsub_rn(1.0f, eps));
+            const double ed = static_cast<double>(e);
+            const float C = static_cast<float>(log((1.0 - ed) / ed));
+            sF = exp(static_cast<double>(C));
+            sTheta = b.bestTheta;
+            sPar = b.bestParity;
+            sLeft = b.bestParity > 0 ? -C : C;
+            sRight = b.bestParity > 0 ? C : -C;
+            sfeat = feats[b.featureIdx];
+            if (weakOut) {
+                vj_weak_classifier wc;
+                wc.featureIdx = b.featureIdx;
+                wc.theta = b.bestTheta;
+                wc.parity = b.bestParity;
+                wc.pad0 = wc.pad1 = wc.pad2 = 0;
+                wc.err = e;
+                wc.alpha = C;
+                wc.leftVal = sLeft;
+                wc.rightVal = sRight;
+                *weakOut = wc;
+            }
+            if (usedMask) usedMask[b.featureIdx] = 1;
+        }
+        if (status) *status = valid ? 0 : 1;
+    }
+    __syncthreads();
+    if (!sValid) return;
+    const vj_haar_feature f = sfeat;
+    const float theta = sTheta, left = sLeft, right = sRight;
+    const double F = sF;
+    const int par = sPar;
+    uint64_t mis = 0;  // n <= 65535 -> at most 64 samples per thread
+    double acc = 0.0;
+    for (int i = tid, j = 0; i < n; i += 1024, ++j) {
+        const float r = train_response(f, sumT, n, i, invNorm[i]);
+        const bool lt = r < theta;
+        strong[i] = __fadd_rn(strong[i], lt ? left : right);
+        const bool act = active == nullptr || active[i] != 0;
+        if (!act) continue;
+        const int pred = par > 0 ? (lt ? -1 : 1) : (lt ? 1 : -1);
+        const bool m = pred != static_cast<int>(label[i]);
+        double x = static_cast<double>(weight[i]);
+        if (m) {
+            mis |= 1ull << j;
+            x = x * F;
+        }
+        acc += x;
+    }
+    part[tid] = acc;
+    __syncthreads();
+    for (int s = 512; s >= 1; s >>= 1) {
+        if (tid < s) part[tid] = part[tid] + part[tid + s];
+        __syncthreads();
+    }
+    const double Z = part[0];
+    for (int i = tid, j = 0; i < n; i += 1024, ++j) {
+        const bool act = active == nullptr || active[i] != 0;
+        double x = 0.0;
+        if (act) {
+            x = static_cast<double>(weight[i]);
+            if ((mis >> j) & 1ull) x = x * F;
+        }
+        weight[i] = (Z > 1e-30) ? static_cast<float>(x / Z) : static_cast<float>(x);
+    }
+}
+
+// Stage calibration (main.cu:2168-2300) in one CTA: radix select of the
+// cutIdx-th smallest positive score in DeviceRadixSort order, then the four
+// counts of CountPassAndNegKernel (main.cu:935-958).
+__global__ void __launch_bounds__(1024)
+stage_calib_kernel(const float* __restrict__ strong, const uint8_t* __restrict__ active, int n,
+                   int numPos, float minHitRate, float maxFalseAlarm, int stageNegBase,
+                   vj_stage_calib* __restrict__ out) {
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t sPrefix, sK;
+    __shared__ int cnt[4];
+    const int tid = threadIdx.x;
+    const int need = static_cast<int>(ceilf(__fmul_rn(minHitRate, static_cast<float>(numPos))));
+    const int minPass = need > 1 ? need : 1;
+    const int cutIdx = numPos - minPass;
+    if (tid == 0) {
+        sPrefix = 0;
+        sK = static_cast<uint32_t>(cutIdx < 0 ? 0 : cutIdx);
+    }
+    __syncthreads();
+    for (int pass = 3; pass >= 0; --pass) {
+        const int shift = pass * 8;
+        for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+        const uint32_t prefix = sPrefix;
+        const uint32_t himask = pass == 3 ? 0u : (0xFFFFFFFFu << (shift + 8));
+        for (int i = tid; i < numPos; i += blockDim.x) {
+            const uint32_t k = radix_key(__float_as_uint(strong[i]));
+            if ((k & himask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t kk = sK, d = 0;
+            while (d < 255 && hist[d] <= kk) {
+                kk -= hist[d];
+                ++d;
+            }
+            sK = kk;
+            sPrefix = prefix | (d << shift);
+        }
+        __syncthreads();
+    }
+    const uint32_t kb = sPrefix;
+    const uint32_t bits = (kb & 0x80000000u) ? (kb ^ 0x80000000u) : ~kb;
+    const float cut = __uint_as_float(bits);
+    if (tid < 4) cnt[tid] = 0;
+    __syncthreads();
+    int pge = 0, pgt = 0, nge = 0, ngt = 0;
+    for (int i = tid; i < n; i += blockDim.x) {
+        const float s = strong[i];
+        if (i < numPos) {
+            pge += s >= cut;
+            pgt += s > cut;
+        } else if (active == nullptr || active[i] != 0) {
+            nge += s >= cut;
+            ngt += s > cut;
+        }
+    }
+    atomicAdd(&cnt[0], pge);
+    atomicAdd(&cnt[1], pgt);
+    atomicAdd(&cnt[2], nge);
+    atomicAdd(&cnt[3], ngt);
+    __syncthreads();
+    if (tid == 0) {
+        const bool strictGt = cnt[1] >= minPass;
+        vj_stage_calib r;
+        r.cutVal = cut;
+        r.stageThreshold = strictGt ? nextafterf(cut, INFINITY) : cut;
+        r.strictGt = strictGt ? 1 : 0;
+        r.posPass = strictGt ? cnt[1] : cnt[0];
+        r.negSurvive = strictGt ? cnt[3] : cnt[2];
+        r.hitRate = __fdiv_rn(static_cast<float>(r.posPass), static_cast<float>(numPos));
+        r.falseAlarm = __fdiv_rn(static_cast<float>(r.negSurvive), static_cast<float>(stageNegBase));
+        r.satisfied = ((r.hitRate >= minHitRate && r.falseAlarm <= maxFalseAlarm) || r.negSurvive == 0) ? 1 : 0;
+        *out = r;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reference step API (AdaBoostTrainer members).
+// ---------------------------------------------------------------------------
+__global__ void eval_responses_kernel(const vj_haar_feature* __restrict__ feats, int featBegin,
+                                      int featCount, const uint32_t* __restrict__ sumT,
+                                      const float* __restrict__ invNorm, int n, float* __restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int fl = blockIdx.y;
+    if (s >= n || fl >= featCount) return;
+    const vj_haar_feature f = feats[featBegin + fl];
+    out[static_cast<size_t>(fl) * n + s] = train_response(f, sumT, n, s, __ldg(invNorm + s));
+}
+
+struct SplitBest {
+    float err;
+    int split;
+    int parity;
+};
+
+// betterBest, boosting_core.cu:59-79: err, then smaller split, then parity +1.
+__device__ __forceinline__ SplitBest better(const SplitBest& a, const SplitBest& b) {
+    if (b.err < a.err) return b;
+    if (b.err > a.err) return a;
+    if (b.split < a.split) return b;
+    if (b.split > a.split) return a;
+    return b.parity > a.parity ? b : a;
+}
+
+// EvaluateAndFindThresholdKernel (boosting_core.cu:289-456) semantics with the
+// prefix sums of sweep_kernel; one warp per feature.
+__global__ void __launch_bounds__(256)
+find_thresholds_kernel(const float* __restrict__ resp, const uint16_t* __restrict__ sorted, int n,
+                       int featCount, const float* __restrict__ wsg, const RoundParams* __restrict__ prm,
+                       vj_feature_best_split* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (f >= featCount) return;
+    const float* rrow = resp + static_cast<size_t>(f) * n;
+    const uint16_t* orow = sorted + static_cast<size_t>(f) * n;
+    const float TP = prm->tp, TN = prm->tn;
+    SplitBest best{FLT_MAX, -1, 1};
+    float cp = 0.0f, cn = 0.0f, kp = 0.0f, kn = 0.0f;
+    for (int base = 0; base < n - 1; base += 256) {
+        const int k0 = base + lane * 8;
+        float lp[8], ln[8];
+        bool ok[8];
+        float sp = 0.0f, sn = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int k = k0 + i;
+            float x = 0.0f;
+            ok[i] = false;
+            if (k < n) {
+                const int s = orow[k];
+                x = wsg[s];
+                if (k + 1 < n) ok[i] = __fadd_rn(rrow[s], 1e-7f) < rrow[orow[k + 1]];
+            }
+            sp = __fadd_rn(sp, fmaxf(x, 0.0f));
+            sn = __fadd_rn(sn, fmaxf(-x, 0.0f));
+            lp[i] = sp;
+            ln[i] = sn;
+        }
+        float ip = sp, in = sn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float yp = __shfl_up_sync(0xffffffffu, ip, o);
+            const float yn = __shfl_up_sync(0xffffffffu, in, o);
+            if (lane >= o) {
+                ip = __fadd_rn(ip, yp);
+                in = __fadd_rn(in, yn);
+            }
+        }
+        float ep = __shfl_up_sync(0xffffffffu, ip, 1), en = __shfl_up_sync(0xffffffffu, in, 1);
+        if (lane == 0) ep = en = 0.0f;
+        const float totp = __shfl_sync(0xffffffffu, ip, 31), totn = __shfl_sync(0xffffffffu, in, 31);
+        const float bp = __fadd_rn(cp, ep), bn = __fadd_rn(cn, en);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (ok[i]) {
+                const float Lp = __fadd_rn(bp, lp[i]), Ln = __fadd_rn(bn, ln[i]);
+                const float eP = __fadd_rn(Ln, __fsub_rn(TP, Lp));
+                const float eN = __fadd_rn(Lp, __fsub_rn(TN, Ln));
+                best = better(best, SplitBest{eP, k0 + i, -1});
+                best = better(best, SplitBest{eN, k0 + i, 1});
+            }
+        }
+        {
+            const float y = __fsub_rn(totp, kp), t = __fadd_rn(cp, y);
+            kp = __fsub_rn(__fsub_rn(t, cp), y);
+            cp = t;
+        }
+        {
+            const float y = __fsub_rn(totn, kn), t = __fadd_rn(cn, y);
+            kn = __fsub_rn(__fsub_rn(t, cn), y);
+            cn = t;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        SplitBest other{__shfl_xor_sync(0xffffffffu, best.err, o), __shfl_xor_sync(0xffffffffu, best.split, o),
+                        __shfl_xor_sync(0xffffffffu, best.parity, o)};
+        best = better(best, other);
+    }
+    if (lane == 0) {
+        vj_feature_best_split r;
+        r.pad0 = r.pad1 = r.pad2 = 0;
+        if (best.split >= 0 && best.split < n - 1) {
+            r.bestErr = best.err;
+            r.bestSplitPos = best.split;
+            r.bestParity = static_cast<int8_t>(best.parity);
+            r.bestTheta = __fmul_rn(0.5f, __fadd_rn(rrow[orow[best.split]], rrow[orow[best.split + 1]]));
+        } else {
+            r.bestErr = FLT_MAX;
+            r.bestSplitPos = best.split;
+            r.bestParity = 1;
+            r.bestTheta = 0.0f;
+        }
+        out[f] = r;
+    }
+}
+
+// SelectBestInTileKernel (boosting_core.cu:155-192): err, then lower featureIdx.
+__global__ void __launch_bounds__(256)
+select_tile_kernel(const vj_feature_best_split* __restrict__ best, int featBegin, int featCount,
+                   const uint8_t* __restrict__ usedMask, vj_tile_best* __restrict__ out) {
+    __shared__ float se[256];
+    __shared__ int sf[256];
+    __shared__ float st[256];
+    __shared__ int sp[256];
+    float e = FLT_MAX, th = 0.0f;
+    int fi = INT_MAX, par = 1;
+    for (int i = threadIdx.x; i < featCount; i += blockDim.x) {
+        const int g = featBegin + i;
+        if (usedMask && usedMask[g]) continue;
+        const vj_feature_best_split b = best[i];
+        if (b.bestErr < e || (b.bestErr == e && g < fi)) {
+            e = b.bestErr;
+            th = b.bestTheta;
+            fi = g;
+            par = b.bestParity;
+        }
+    }
+    se[threadIdx.x] = e;
+    sf[threadIdx.x] = fi;
+    st[threadIdx.x] = th;
+    sp[threadIdx.x] = par;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            const int o = threadIdx.x + s;
+            if (se[o] < se[threadIdx.x] || (se[o] == se[threadIdx.x] && sf[o] < sf[threadIdx.x])) {
+                se[threadIdx.x] = se[o];
+                sf[threadIdx.x] = sf[o];
+                st[threadIdx.x] = st[o];
+                sp[threadIdx.x] = sp[o];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        vj_tile_best r;
+        r.bestErr = se[0];
+        r.bestTheta = st[0];
+        r.featureIdx = sf[0];
+        r.bestParity = static_cast<int8_t>(sp[0]);
+        r.pad0 = r.pad1 = r.pad2 = 0;
+        *out = r;
+    }
+}
+
+int sm_count() {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cached = v > 0 ? v : 1;
+    }
+    return cached;
+}
+
+// Launches eval_sort_kernel with the smallest items-per-thread that holds n.
+int launch_eval_sort(const vj_haar_feature* feats, int featBegin, int featCount, const uint32_t* sumT,
+                     const float* invNorm, int n, const float* resp, uint16_t* ordOut, int64_t ordStride,
+                     bool ordPadded, uint32_t* gapOut, int64_t gapStride, cudaStream_t stream) {
+    const int grid = std::min(featCount, sm_count());
+    auto go = [&](auto kernel, size_t smem) -> int {
+        VJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        VJ_TIMED_LAUNCH("eval_sort_kernel", stream,
+                        kernel<<<grid, kSortThreads, smem, stream>>>(feats, featBegin, featCount, sumT, invNorm, n,
+                                                                     resp, ordOut, ordStride, ordPadded, gapOut,
+                                                                     gapStride));
+        VJ_LAUNCH_CHECK("eval_sort_kernel");
+        return VJ_OK;
+    };
+#define VJ_SORT_CASE(RR)                                                                   \
+    if (n <= 1024 * RR)                                                                    \
+        return resp ? go(eval_sort_kernel<RR, true>, sort_smem_bytes<RR>())                \
+                    : go(eval_sort_kernel<RR, false>, sort_smem_bytes<RR>());
+    VJ_SORT_CASE(4)
+    VJ_SORT_CASE(8)
+    VJ_SORT_CASE(16)
+    VJ_SORT_CASE(20)
+    VJ_SORT_CASE(24)
+    VJ_SORT_CASE(32)
+#undef VJ_SORT_CASE
+    return set_error(VJ_INVALID_ARG, "on-chip sort holds at most 32768 samples per feature");
+}
+
+}  // namespace
+}  // namespace vjgb
+
+using namespace vjgb;
+
+struct vj_trainer {
+    int winW = 24, winH = 24, maxSamples = 0;
+    vj_haar_feature* d_feat = nullptr;
+    int64_t nFeat = 0;
+    const uint32_t* d_sumT = nullptr;
+    const float* d_invNorm = nullptr;
+    int n = 0;
+    const int8_t* d_label = nullptr;
+    const uint8_t* d_active = nullptr;
+    float* d_weight = nullptr;
+    // Per-feature sample orders and valid-split masks.
+    uint16_t* d_ord = nullptr;
+    uint32_t* d_gap = nullptr;
+    size_t ordBytes = 0, gapBytes = 0;
+    int64_t ordStride = 0, gapStride = 0;
+    bool prepared = false;
+    // Per-round scratch.
+    float* d_wsg = nullptr;
+    float* d_fastErr = nullptr;
+    int* d_cand = nullptr;
+    int8_t* d_refParity = nullptr;
+    int* d_refSplit = nullptr;
+    RoundParams* d_prm = nullptr;
+    int* d_status = nullptr;
+    int64_t scratchFeat = 0;
+    int scratchN = 0;
+};
+
+namespace {
+
+int ensure_round_scratch(vj_trainer* t) {
+    if (t->scratchFeat >= t->nFeat && t->scratchN >= t->n && t->d_prm) return VJ_OK;
+    cudaFree(t->d_wsg);
+    cudaFree(t->d_fastErr);
+    cudaFree(t->d_cand);
+    cudaFree(t->d_refParity);
+    cudaFree(t->d_refSplit);
+    t->d_wsg = nullptr;
+    t->d_fastErr = nullptr;
+    t->d_cand = nullptr;
+    t->d_refParity = nullptr;
+    t->d_refSplit = nullptr;
+    t->scratchFeat = t->scratchN = 0;
+    const int64_t F = t->nFeat > 0 ? t->nFeat : 1;
+    const int N = t->maxSamples;
+    VJ_CUDA_TRY(cudaMalloc(&t->d_wsg, sizeof(float) * N));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_fastErr, sizeof(float) * F));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_cand, sizeof(int) * F));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_refParity, F));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_refSplit, sizeof(int) * F));
+    if (!t->d_prm) VJ_CUDA_TRY(cudaMalloc(&t->d_prm, sizeof(RoundParams)));
+    if (!t->d_status) VJ_CUDA_TRY(cudaMalloc(&t->d_status, sizeof(int)));
+    t->scratchFeat = F;
+    t->scratchN = N;
+    return VJ_OK;
+}
+
+int check_bound(vj_trainer* t, const char* fn) {
+    if (!t) return set_error(VJ_INVALID_ARG, std::string(fn) + ": null trainer");
+    if (!t->d_feat || t->nFeat <= 0) return set_error(VJ_INVALID_ARG, std::string(fn) + ": no feature pool set");
+    if (!t->d_sumT || t->n <= 0) return set_error(VJ_INVALID_ARG, std::string(fn) + ": no training set bound");
+    return VJ_OK;
+}
+
+// Writes the per-feature orders and split masks for the whole pool.
+int sort_all(vj_trainer* t, cudaStream_t s) {
+    const int64_t ordStride = (t->n + 7) & ~7;
+    const int64_t gapStride = (t->n + 31) / 32;
+    const size_t ordBytes = static_cast<size_t>(t->nFeat) * ordStride * sizeof(uint16_t);
+    const size_t gapBytes = static_cast<size_t>(t->nFeat) * gapStride * sizeof(uint32_t);
+    if (ordBytes > t->ordBytes) {
+        cudaFree(t->d_ord);
+        t->d_ord = nullptr;
+        t->ordBytes = 0;
+        VJ_CUDA_TRY(cudaMalloc(&t->d_ord, ordBytes));
+        t->ordBytes = ordBytes;
+    }
+    if (gapBytes > t->gapBytes) {
+        cudaFree(t->d_gap);
+        t->d_gap = nullptr;
+        t->gapBytes = 0;
+        VJ_CUDA_TRY(cudaMalloc(&t->d_gap, gapBytes));
+        t->gapBytes = gapBytes;
+    }
+    t->ordStride = ordStride;
+    t->gapStride = gapStride;
+    return launch_eval_sort(t->d_feat, 0, static_cast<int>(t->nFeat), t->d_sumT, t->d_invNorm, t->n, nullptr,
+                            t->d_ord, ordStride, true, t->d_gap, gapStride, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int vj_trainer_create(int winW, int winH, int maxSamples, vj_trainer** out) {
+    if (!out) return set_error(VJ_INVALID_ARG, "vj_trainer_create: null out");
+    *out = nullptr;
+    if (winW != kWin || winH != kWin)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_create: the training window is 24x24");
+    if (maxSamples <= 1 || maxSamples > kMaxSamples)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_create: maxSamples must be in [2, 65535]");
+    auto* t = new vj_trainer();
+    t->winW = winW;
+    t->winH = winH;
+    t->maxSamples = maxSamples;
+    *out = t;
+    return ok();
+}
+
+int vj_trainer_destroy(vj_trainer* t) {
+    if (!t) return ok();
+    cudaFree(t->d_feat);
+    cudaFree(t->d_ord);
+    cudaFree(t->d_gap);
+    cudaFree(t->d_wsg);
+    cudaFree(t->d_fastErr);
+    cudaFree(t->d_cand);
+    cudaFree(t->d_refParity);
+    cudaFree(t->d_refSplit);
+    cudaFree(t->d_prm);
+    cudaFree(t->d_status);
+    delete t;
+    return ok();
+}
+
+int vj_trainer_set_features(vj_trainer* t, const vj_haar_feature* features, int64_t count) {
+    if (!t || !features || count <= 0 || count > INT_MAX)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_set_features: bad arguments");
+    for (int64_t i = 0; i < count; ++i) {
+        const vj_haar_feature& f = features[i];
+        const vj_fast_rect* rr[3] = {&f.r0, &f.r1, &f.r2};
+        if (f.tilted || (f.rectCount != 2 && f.rectCount != 3))
+            return set_error(VJ_INVALID_ARG, "vj_trainer_set_features: only upright 2/3-rect features train");
+        for (int r = 0; r < f.rectCount; ++r) {
+            const int32_t p[4] = {rr[r]->p0, rr[r]->p1, rr[r]->p2, rr[r]->p3};
+            for (int c = 0; c < 4; ++c)
+                if (p[c] < 0 || p[c] >= kIIArea)
+                    return set_error(VJ_INVALID_ARG, "vj_trainer_set_features: corner outside the 25x25 integral");
+        }
+    }
+    cudaFree(t->d_feat);
+    t->d_feat = nullptr;
+    t->nFeat = 0;
+    t->prepared = false;
+    VJ_CUDA_TRY(cudaMalloc(&t->d_feat, sizeof(vj_haar_feature) * count));
+    VJ_CUDA_TRY(cudaMemcpy(t->d_feat, features, sizeof(vj_haar_feature) * count, cudaMemcpyHostToDevice));
+    t->nFeat = count;
+    return ok();
+}
+
+int vj_trainer_bind(vj_trainer* t, const uint32_t* d_sumT, const float* d_invNorm, int n,
+                    const int8_t* d_label, const uint8_t* d_active, float* d_weight) {
+    if (!t || !d_sumT || !d_invNorm || !d_label || !d_weight)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_bind: null view");
+    if (n <= 1 || n > t->maxSamples)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_bind: sample count outside [2, maxSamples]");
+    t->d_sumT = d_sumT;
+    t->d_invNorm = d_invNorm;
+    t->n = n;
+    t->d_label = d_label;
+    t->d_active = d_active;
+    t->d_weight = d_weight;
+    t->prepared = false;
+    return ok();
+}
+
+int vj_trainer_stage_bytes(vj_trainer* t, int n, int64_t* bytes) {
+    if (!t || !bytes || n <= 0) return set_error(VJ_INVALID_ARG, "vj_trainer_stage_bytes: bad arguments");
+    *bytes = t->nFeat * (((n + 7) & ~7) * 2 + ((n + 31) / 32) * 4);
+    return ok();
+}
+
+int vj_trainer_prepare_stage(vj_trainer* t, void* stream) {
+    int st = check_bound(t, "vj_trainer_prepare_stage");
+    if (st != VJ_OK) return st;
+    st = sort_all(t, static_cast<cudaStream_t>(stream));
+    if (st != VJ_OK) return st;
+    t->prepared = true;
+    return ok();
+}
+
+int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_out, void* stream) {
+    int st = check_bound(t, "vj_stump_search");
+    if (st != VJ_OK) return st;
+    if (!d_out) return set_error(VJ_INVALID_ARG, "vj_stump_search: null output");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!t->prepared) {
+        st = sort_all(t, s);
+        if (st != VJ_OK) return st;
+    }
+    st = ensure_round_scratch(t);
+    if (st != VJ_OK) return st;
+    const int F = static_cast<int>(t->nFeat), n = t->n;
+    VJ_TIMED_LAUNCH("prep_round_kernel", s,
+                    prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, n, t->d_wsg, t->d_prm));
+    VJ_LAUNCH_CHECK("prep_round_kernel");
+    const bool smemW = n <= kSmemWeightsMax;
+    const size_t wbytes = smemW ? sizeof(float) * n : 0;
+    {
+        const int grid = std::min(div_up(F, kSweepWarps), 2 * sm_count());
+        auto k = smemW ? sweep_kernel<true> : sweep_kernel<false>;
+        VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
+        VJ_TIMED_LAUNCH("sweep_kernel", s,
+                        k<<<grid, kSweepThreads, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride,
+                                                             t->d_wsg, n, F, d_usedMask, t->d_prm, t->d_fastErr));
+        VJ_LAUNCH_CHECK("sweep_kernel");
+    }
+    VJ_TIMED_LAUNCH("select_candidates_kernel", s,
+                    select_candidates_kernel<<<std::min(div_up(F, 256), 4 * sm_count()), 256, 0, s>>>(
+                        t->d_fastErr, F, t->d_prm, t->d_cand));
+    VJ_LAUNCH_CHECK("select_candidates_kernel");
+    {
+        auto k = smemW ? refine_kernel<true> : refine_kernel<false>;
+        VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
+        VJ_TIMED_LAUNCH("refine_kernel", s,
+                        k<<<sm_count(), 256, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg,
+                                                          n, t->d_prm, t->d_cand, t->d_refParity, t->d_refSplit));
+        VJ_LAUNCH_CHECK("refine_kernel");
+    }
+    VJ_TIMED_LAUNCH("finalize_kernel", s,
+                    finalize_kernel<<<1, 32, 0, s>>>(t->d_feat, t->d_sumT, t->d_invNorm, n, t->d_ord, t->ordStride,
+                                                     t->d_prm, t->d_refParity, t->d_refSplit, d_out));
+    VJ_LAUNCH_CHECK("finalize_kernel");
+    return ok();
+}
+
+int vj_round_update(vj_trainer* t, const vj_tile_best* d_best, float* d_strong, uint8_t* d_usedMask,
+                    vj_weak_classifier* d_weak_out, void* stream) {
+    int st = check_bound(t, "vj_round_update");
+    if (st != VJ_OK) return st;
+    if (!d_best || !d_strong) return set_error(VJ_INVALID_ARG, "vj_round_update: null argument");
+    st = ensure_round_scratch(t);
+    if (st != VJ_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VJ_TIMED_LAUNCH("round_update_kernel", s,
+                    round_update_kernel<<<1, 1024, 0, s>>>(t->d_feat, d_best, t->d_sumT, t->d_invNorm, t->d_label,
+                                                           t->d_active, t->d_weight, d_strong, t->n, d_usedMask,
+                                                           d_weak_out, t->d_status));
+    VJ_LAUNCH_CHECK("round_update_kernel");
+    return ok();
+}
+
+int vj_stage_calibrate(vj_trainer* t, const float* d_strong, int numPos, float minHitRate, float maxFalseAlarm,
+                       int stageNegBaseCount, vj_stage_calib* d_out, void* stream) {
+    if (!t || !d_strong || !d_out || t->n <= 0)
+        return set_error(VJ_INVALID_ARG, "vj_stage_calibrate: bad arguments");
+    if (numPos <= 0 || numPos > t->n || stageNegBaseCount <= 0 || !(minHitRate > 0.0f && minHitRate <= 1.0f))
+        return set_error(VJ_INVALID_ARG, "vj_stage_calibrate: bad counts or hit rate");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VJ_TIMED_LAUNCH("stage_calib_kernel", s,
+                    stage_calib_kernel<<<1, 1024, 0, s>>>(d_strong, t->d_active, t->n, numPos, minHitRate,
+                                                          maxFalseAlarm, stageNegBaseCount, d_out));
+    VJ_LAUNCH_CHECK("stage_calib_kernel");
+    return ok();
+}
+
+int vj_trainer_evaluate_responses(vj_trainer* t, int featureBegin, int featureCount, float* d_out, void* stream) {
+    int st = check_bound(t, "vj_trainer_evaluate_responses");
+    if (st != VJ_OK) return st;
+    if (!d_out || featureBegin < 0 || featureCount <= 0 || featureBegin + static_cast<int64_t>(featureCount) > t->nFeat ||
+        featureCount > 65535)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_evaluate_responses: bad feature range");
+    const dim3 grid(div_up(t->n, 256), featureCount);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VJ_TIMED_LAUNCH("eval_responses_kernel", s,
+                    eval_responses_kernel<<<grid, 256, 0, s>>>(t->d_feat, featureBegin, featureCount, t->d_sumT,
+                                                               t->d_invNorm, t->n, d_out));
+    VJ_LAUNCH_CHECK("eval_responses_kernel");
+    return ok();
+}
+
+int vj_trainer_sort_per_feature(vj_trainer* t, const float* d_resp, int featureCount, uint16_t* d_sortedIdx,
+                                void* stream) {
+    if (!t || !d_resp || !d_sortedIdx || featureCount <= 0 || t->n <= 0)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_sort_per_feature: bad arguments");
+    const int st = launch_eval_sort(nullptr, 0, featureCount, nullptr, nullptr, t->n, d_resp, d_sortedIdx, t->n,
+                                    false, nullptr, 0, static_cast<cudaStream_t>(stream));
+    return st == VJ_OK ? ok() : st;
+}
+
+int vj_trainer_find_thresholds(vj_trainer* t, const float* d_resp, const uint16_t* d_sortedIdx, int featureCount,
+                               vj_feature_best_split* d_out, void* stream) {
+    int st = check_bound(t, "vj_trainer_find_thresholds");
+    if (st != VJ_OK) return st;
+    if (!d_resp || !d_sortedIdx || !d_out || featureCount <= 0)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_find_thresholds: bad arguments");
+    st = ensure_round_scratch(t);
+    if (st != VJ_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VJ_TIMED_LAUNCH("prep_round_kernel", s,
+                    prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, t->n, t->d_wsg,
+                                                         t->d_prm));
+    VJ_LAUNCH_CHECK("prep_round_kernel");
+    VJ_TIMED_LAUNCH("find_thresholds_kernel", s,
+                    find_thresholds_kernel<<<div_up(featureCount, 8), 256, 0, s>>>(d_resp, d_sortedIdx, t->n,
+                                                                                  featureCount, t->d_wsg, t->d_prm,
+                                                                                  d_out));
+    VJ_LAUNCH_CHECK("find_thresholds_kernel");
+    return ok();
+}
+
+int vj_trainer_select_best_in_tile(vj_trainer* t, const vj_feature_best_split* d_best, int featureBegin,
+                                   int featureCount, const uint8_t* d_usedMask, vj_tile_best* d_out, void* stream) {
+    if (!t || !d_best || !d_out || featureBegin < 0 || featureCount <= 0)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_select_best_in_tile: bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VJ_TIMED_LAUNCH("select_tile_kernel", s,
+                    select_tile_kernel<<<1, 256, 0, s>>>(d_best, featureBegin, featureCount, d_usedMask, d_out));
+    VJ_LAUNCH_CHECK("select_tile_kernel");
+    return ok();
+}
+
+}  // extern "C"

@@ -1,0 +1,296 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the oracle and
+the reference's golden outputs.  Integer work is compared bit for bit; stump
+picks (feature, threshold, parity, FP32 error) too."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import f32
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+# ---------------------------------------------------------------- integrals
+def test_integral_batch_24(cuda, vj, oracle):
+    torch = cuda
+    p = vj.synth_patches(9, 300, 300)
+    p[3] = 17
+    p[400] = 255
+    d = dev(torch, p)
+    n = len(p)
+    sumT = torch.empty(625 * n, dtype=torch.int32, device="cuda")
+    sqT = torch.empty(625 * n, dtype=torch.int64, device="cuda")
+    inv = torch.empty(n, dtype=torch.float32, device="cuda")
+    vj._capi.call("vj_integral_batch", d.data_ptr(), 24, 24, 24, n, sumT.data_ptr(), sqT.data_ptr(), inv.data_ptr(), None)
+    torch.cuda.synchronize()
+    sums, oinv = oracle.train_integrals(p)
+    assert np.array_equal(sumT.cpu().numpy().view(np.uint32).reshape(625, n).T, sums)
+    assert np.array_equal(inv.cpu().numpy().view(np.uint32), oinv.view(np.uint32))
+    for i in (0, 3, 400):
+        _, q = oracle.integral(p[i])
+        assert np.array_equal(sqT.cpu().numpy().view(np.uint64).reshape(625, n)[:, i], q.ravel())
+
+
+@pytest.mark.parametrize("h,w", [(7, 5), (31, 40)])
+def test_integral_batch_generic(cuda, vj, oracle, h, w):
+    torch = cuda
+    rng = np.random.default_rng(h * w)
+    n = 77
+    imgs = rng.integers(0, 256, (n, h, w), dtype=np.uint8)
+    d = dev(torch, imgs)
+    area = (h + 1) * (w + 1)
+    sumT = torch.empty(area * n, dtype=torch.int32, device="cuda")
+    sqT = torch.empty(area * n, dtype=torch.int64, device="cuda")
+    inv = torch.empty(n, dtype=torch.float32, device="cuda")
+    vj._capi.call("vj_integral_batch", d.data_ptr(), w, h, w, n, sumT.data_ptr(), sqT.data_ptr(), inv.data_ptr(), None)
+    S = sumT.cpu().numpy().view(np.uint32).reshape(area, n)
+    Q = sqT.cpu().numpy().view(np.uint64).reshape(area, n)
+    for i in (0, 41, 76):
+        s, q = oracle.integral(imgs[i])
+        assert np.array_equal(S[:, i], s.ravel()) and np.array_equal(Q[:, i], q.ravel())
+
+
+@pytest.mark.parametrize("h,w", [(1, 1), (24, 24), (61, 97), (300, 400), (480, 640), (1080, 1920), (2160, 3840)])
+def test_integral_image(cuda, vj, oracle, h, w):
+    torch = cuda
+    img = vj.synth_scene(h * 7 + w, w, h, 0) if min(h, w) >= 24 else np.full((h, w), 255, np.uint8)
+    if (h, w) == (300, 400):
+        img[:] = 255  # sums beyond 2^24, squared sums beyond 2^32
+    d = dev(torch, img)
+    s = torch.empty((h + 1) * (w + 1), dtype=torch.int32, device="cuda")
+    q = torch.empty((h + 1) * (w + 1), dtype=torch.int64, device="cuda")
+    vj._capi.call("vj_integral_image", d.data_ptr(), w, h, w, s.data_ptr(), q.data_ptr(), None)
+    os_, oq = oracle.integral(img)
+    assert np.array_equal(s.cpu().numpy().view(np.uint32), os_.ravel())
+    assert np.array_equal(q.cpu().numpy().view(np.uint64), oq.ravel())
+
+
+# ---------------------------------------------------------------- stump search
+class Train:
+    """A bound trainer over patches (positives first) with device buffers."""
+
+    def __init__(self, torch, vj, oracle, patches, labels, feats, weights, active=None):
+        self.torch, self.vj = torch, vj
+        n = len(labels)
+        self.n = n
+        self.d_p = dev(torch, patches)
+        self.sumT = torch.empty(625 * n, dtype=torch.int32, device="cuda")
+        self.inv = torch.empty(n, dtype=torch.float32, device="cuda")
+        vj._capi.call("vj_integral_batch", self.d_p.data_ptr(), 24, 24, 24, n, self.sumT.data_ptr(), None,
+                      self.inv.data_ptr(), None)
+        self.lab = dev(torch, labels.astype(np.int8))
+        self.act = dev(torch, active) if active is not None else None
+        self.w = dev(torch, weights.astype(np.float32))
+        self.t = vj.AdaBoostTrainer((24, 24), n)
+        assert self.t.setFeaturePool(feats.view(vj.HAAR_FEATURE)) == 0
+        ii = dict(nSamples=n, d_sumT=self.sumT, d_invNorm=self.inv)
+        assert self.t.bindTrainingSet(ii, self.lab, self.act, self.w) == 0
+        self.best = torch.zeros(4, dtype=torch.int32, device="cuda")
+        self.used = torch.zeros(len(feats), dtype=torch.uint8, device="cuda")
+        self.strong = torch.zeros(n, dtype=torch.float32, device="cuda")
+
+    def search(self, used=False):
+        assert self.t.bestWeak(self.used if used else None, self.best) == 0
+        b = self.best.cpu().numpy().view(self.vj.TILE_BEST)[0]
+        return int(b["featureIdx"]), float(b["bestErr"]), float(b["bestTheta"]), int(b["bestParity"])
+
+
+def test_weak_search_golden_cases(cuda, vj, oracle, golden, gin, basic_pool):
+    patches = gin["ws_patches"]
+    labels = np.array([1] * 160 + [-1] * 160, np.int8)
+    for g in golden["weak_search"]:
+        idx = gin[g["key"] + "_idx"]
+        T = Train(cuda, vj, oracle, patches, labels, np.ascontiguousarray(basic_pool[idx]), gin[g["key"] + "_w"],
+                  gin.get(g["key"] + "_active"))
+        got = T.search()
+        assert got == (g["featureIdx"], f32(g["err_bits"]), f32(g["theta_bits"]), g["parity"]), g
+
+
+def test_weak_search_resident_equals_fused(cuda, vj, oracle, gin, basic_pool):
+    patches = gin["ws_patches"]
+    labels = np.array([1] * 160 + [-1] * 160, np.int8)
+    rng = np.random.default_rng(4)
+    w = (rng.random(320) / 320).astype(np.float32)
+    T = Train(cuda, vj, oracle, patches, labels, np.ascontiguousarray(basic_pool[:20000]), w)
+    fused = T.search()
+    assert T.t.prepareStage() == 0
+    assert T.search() == fused
+
+
+def test_rounds_match_reference_and_oracle(cuda, vj, oracle, golden, basic_pool):
+    g = golden["rounds"]
+    p = vj.synth_patches(g["seed"], g["npos"], g["nneg"])
+    labels = np.array([1] * g["npos"] + [-1] * g["nneg"], np.int8)
+    feats = np.ascontiguousarray(basic_pool[: g["features"]])
+    w0 = np.full(len(labels), np.float32(0.5) / np.float32(g["npos"]), np.float32)
+    T = Train(cuda, vj, oracle, p, labels, feats, w0)
+    assert T.t.prepareStage() == 0
+    sums, inv = oracle.train_integrals(p)
+    w = w0.copy()
+    strong = np.zeros(len(labels), np.float32)
+    weak = cuda.zeros(7, dtype=cuda.int32, device="cuda")
+    for r in g["picks"]:
+        got = T.search(used=True)
+        assert got == (r["featureIdx"], f32(r["err_bits"]), f32(r["theta_bits"]), r["parity"])
+        assert T.t.applyBestWeak(T.best, T.strong, T.used, weak) == 0
+        oracle.round_update(feats, dict(featureIdx=got[0], err=got[1], theta=got[2], parity=got[3]), sums, inv,
+                            labels, w, strong)
+        gw = T.w.cpu().numpy()
+        assert np.max(np.abs(gw.view(np.int32).astype(np.int64) - w.view(np.int32).astype(np.int64))) <= 1
+        assert np.array_equal(T.strong.cpu().numpy(), strong)
+        wk = weak.cpu().numpy().view(vj.WEAK)[0]
+        assert wk["featureIdx"] == got[0] and wk["parity"] == got[3]
+        assert wk["leftVal"] == -wk["rightVal"] and (wk["leftVal"] < 0) == (got[3] > 0)
+        w = gw.copy()  # continue from the device weights
+
+
+@pytest.mark.slow
+def test_config0_round1_full_pool(cuda, vj, oracle, golden, basic_pool):
+    g = golden["config0_round1"]
+    p = vj.synth_patches(677, 2000, 2000)
+    labels = np.array([1] * 2000 + [-1] * 2000, np.int8)
+    w = np.full(4000, np.float32(0.5) / np.float32(2000), np.float32)
+    T = Train(cuda, vj, oracle, p, labels, basic_pool, w)
+    want = (g["featureIdx"], f32(g["err_bits"]), f32(g["theta_bits"]), g["parity"])
+    assert T.search() == want
+    assert T.t.prepareStage() == 0
+    assert T.search() == want
+
+
+def test_step_api_matches_oracle(cuda, vj, oracle, gin, basic_pool):
+    torch = cuda
+    patches = gin["ws_patches"]
+    labels = np.array([1] * 160 + [-1] * 160, np.int8)
+    rng = np.random.default_rng(8)
+    w = (rng.random(320) / 320).astype(np.float32)
+    F = 3000
+    feats = np.ascontiguousarray(basic_pool[:F])
+    T = Train(cuda, vj, oracle, patches, labels, feats, w)
+    n = 320
+    resp = torch.empty(F * n, dtype=torch.float32, device="cuda")
+    assert T.t.evaluateFeatureResponses(0, F, resp) == 0
+    sums, inv = oracle.train_integrals(patches)
+    R = resp.cpu().numpy().reshape(F, n)
+    for f in (0, 17, 2999):
+        ref = np.array([oracle.lib().vjo_train_response(feats[f:f + 1].ctypes.data, sums[i].ctypes.data, inv[i])
+                        for i in range(n)], np.float32)
+        assert np.array_equal(R[f].view(np.uint32), ref.view(np.uint32))
+    order = torch.empty(F * n, dtype=torch.int16, device="cuda")
+    assert T.t.sortSamplesPerFeature(resp, F, order) == 0
+    O_ = order.cpu().numpy().view(np.uint16).reshape(F, n)
+    bits = R.view(np.uint32)
+    keys = np.where(bits >> 31, ~bits, bits | np.uint32(0x80000000))
+    for f in range(0, F, 97):
+        assert np.array_equal(O_[f], np.lexsort((np.arange(n), keys[f])))
+    best = torch.empty(F * 4, dtype=torch.int32, device="cuda")
+    assert T.t.evaluateAndFindThreshold(resp, order, F, best) == 0
+    B = best.cpu().numpy().view(vj.FEATURE_BEST)
+    e64 = oracle.feature_err64(feats, sums, inv, labels, w)
+    assert np.allclose(B["bestErr"], e64, rtol=0, atol=1e-6)
+    tile = torch.zeros(4, dtype=torch.int32, device="cuda")
+    assert T.t.selectBestInTile(best, 0, F, None, tile) == 0
+    tb = tile.cpu().numpy().view(vj.TILE_BEST)[0]
+    assert tb["bestErr"] == B["bestErr"].min() and tb["featureIdx"] == int(np.argmin(B["bestErr"]))
+
+
+def test_stage_calibration(cuda, vj, oracle, gin, basic_pool):
+    torch = cuda
+    patches = gin["ws_patches"]
+    labels = np.array([1] * 160 + [-1] * 160, np.int8)
+    T = Train(cuda, vj, oracle, patches, labels, np.ascontiguousarray(basic_pool[:100]),
+              np.full(320, np.float32(1 / 320), np.float32))
+    rng = np.random.default_rng(2)
+    for trial in range(5):
+        strong = rng.normal(size=320).astype(np.float32)
+        if trial == 1:
+            strong[:40] = strong[3]
+        if trial == 2:
+            strong[:] = np.round(strong * 2) / 2
+        d_s = dev(torch, strong)
+        out = torch.zeros(8, dtype=torch.int32, device="cuda")
+        assert T.t.calibrateStage(d_s, 160, 0.99, 0.4, 160, out) == 0
+        got = out.cpu().numpy().view(vj.STAGE_CALIB)[0]
+        ref = oracle.stage_calibrate(strong, 160, np.float32(0.99), np.float32(0.4), 160)
+        for k in ("cutVal", "stageThreshold", "hitRate", "falseAlarm"):
+            assert np.float32(got[k]).tobytes() == np.float32(ref[k]).tobytes(), k
+        for k in ("strictGt", "posPass", "negSurvive", "satisfied"):
+            assert int(got[k]) == ref[k], k
+
+
+# ---------------------------------------------------------------- detection
+def detector(vj, pool, st, sg, w=3840, h=2160, norm=0):
+    e = vj.FaceVisionEngine((24, 24), 1, w, h, False, 200000)
+    assert e.setCascadeModel(pool.view(vj.HAAR_FEATURE), st.view(vj.STUMP4), sg.view(vj.STAGE)) == 0
+    assert e.setNormMode(norm) == 0
+    return e
+
+
+def test_detect_golden(cuda, vj, golden, gin, basic_pool):
+    e = detector(vj, basic_pool, gin["det_stumps"], gin["det_stages"], norm=1)
+    for g in golden["detect"]:
+        scene = gin[f"det_scene_{g['key']}"]
+        st, raw = e.detectMultiScale(scene, g["w"], g["h"], g["w"], 1.25, 4, 24, 200000, applyGrouping=False)
+        assert st == 0 and raw.tobytes() == gin[f"det_raw_{g['key']}"].tobytes()
+        st, grp = e.detectMultiScale(scene, g["w"], g["h"], g["w"], 1.25, 4, 24, 200000, applyGrouping=True)
+        assert st == 0 and grp.tobytes() == gin[f"det_grouped_{g['key']}"].tobytes()
+    st, raw = e.detectMultiScale(gin["det_scene_0"], 320, 240, 320, 1.25, 4, 24, 50, applyGrouping=False)
+    assert raw.tobytes() == gin["det_trunc"].tobytes()
+
+
+@pytest.mark.parametrize("norm", [0, 1])
+def test_detect_1080p_full_cascade(cuda, vj, oracle, basic_pool, norm):
+    st, sg = vj.synth_cascade(2)
+    scene = vj.synth_scene(1, 1920, 1080, 40, 24, 300)
+    e = detector(vj, basic_pool, st, sg, norm=norm)
+    s, raw = e.detectMultiScale(scene, 1920, 1080, 1920, 1.25, 4, 24, 200000, applyGrouping=False)
+    ref = oracle.detect(basic_pool, st, sg, scene, norm_mode=norm, threads=8)
+    assert s == 0 and len(raw) == len(ref) and raw.tobytes() == ref.tobytes()
+    s, grp = e.detectMultiScale(scene, 1920, 1080, 1920, 1.25, 4, 24, 200000)
+    assert grp.tobytes() == oracle.group(ref, 4, 0.2).tobytes()
+
+
+def test_detect_device_image_and_strides(cuda, vj, oracle, basic_pool, gin):
+    torch = cuda
+    st, sg = gin["det_stumps"], gin["det_stages"]
+    scene = gin["det_scene_1"]
+    h, w = scene.shape
+    padded = np.zeros((h, w + 13), np.uint8)
+    padded[:, :w] = scene
+    e = detector(vj, basic_pool, st, sg, norm=1)
+    s1, a = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    s2, b = e.detectMultiScale(dev(torch, padded), w, h, w + 13, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s1 == 0 and s2 == 0 and a.tobytes() == b.tobytes()
+
+
+def test_detect_batch_equals_single(cuda, vj, basic_pool):
+    st, sg = vj.synth_cascade(2)
+    rng = np.random.default_rng(3)
+    scenes = []
+    for k in range(6):
+        t = rng.random()
+        w, h = int(320 * 12 ** t), int(240 * 9 ** t)
+        scenes.append(vj.synth_scene(50 + k, min(w, 1280), min(h, 720), 5, 24, 200))
+    e = detector(vj, basic_pool, st, sg)
+    s, batch = e.detectBatch(scenes, capPerImage=20000)
+    assert s == 0
+    for sc, b in zip(scenes, batch):
+        s, one = e.detectMultiScale(sc, sc.shape[1], sc.shape[0], sc.shape[1], 1.25, 4, 24, 200000)
+        assert s == 0 and one.tobytes() == b.tobytes()
+
+
+def test_detect_rejects_bad_input(cuda, vj, basic_pool, gin):
+    e = vj.FaceVisionEngine((24, 24), 1, 64, 64, False, 1000)
+    img = np.zeros((32, 32), np.uint8)
+    s, _ = e.detectMultiScale(img, 32, 32, 32)
+    assert s == vj.Status.kInvalidArg  # no model
+    e = detector(vj, basic_pool, gin["det_stumps"], gin["det_stages"], w=64, h=64)
+    big = np.zeros((100, 100), np.uint8)
+    assert e.detectMultiScale(big, 100, 100, 100)[0] == vj.Status.kInvalidArg
+    assert e.detectMultiScale(img, 32, 32, 32, scaleFactor=1.0)[0] == vj.Status.kInvalidArg
+    s, d = e.detectMultiScale(np.zeros((20, 20), np.uint8), 20, 20, 20)
+    assert s == 0 and len(d) == 0  # smaller than the window: no level
