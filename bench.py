@@ -176,7 +176,7 @@ def run_gpu(args, rank, world):
     if world > 1:
         import torch.distributed as dist  # noqa: F811
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    pool = V.feature_pool(V.FeatureMode.Basic)
+    pool = V.feature_pool(V.FeatureMode.Basic)[: args.features]
     F = len(pool)
     patches = V.synth_patches(SEED, NPOS, NNEG)
     n = len(patches)
@@ -275,7 +275,9 @@ def run_gpu(args, rank, world):
         "clocks": clk.summary(),
         "picks_head": [int(x) for x in weaks["featureIdx"][:5]],
     }
-    if rank == 0:
+    if F != 162336 or ROUNDS != 50:
+        result["config"]["workload"] = f"reduced stage step for profiling: {F} features, {ROUNDS} rounds"
+    if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(pool, patches)
     if dist:
         dist.destroy_process_group()
@@ -342,7 +344,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--features", type=int, default=162336, help="first K Basic features (profiling cases)")
+    ap.add_argument("--rounds", type=int, default=50, help="boosting rounds per step (profiling cases)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    global ROUNDS
+    ROUNDS = args.rounds
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
