@@ -18,6 +18,7 @@
 // in-place column scan with the carry of the segments above.  All levels of
 // all images of a batch go through one launch of each pass.
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -332,11 +333,88 @@ int launch_integral_jobs(const IIJob* d_jobs, int njobs, const IIPlan& plan, uin
     return VJ_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch of vj_integral_image_noalloc: a fixed array in device memory, sized
+// for the largest image the variant accepts.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxW = 3840, kNoAllocMaxH = 2160;
+constexpr int64_t kNoAllocTotRows = (kNoAllocMaxH + kColSeg - 1) / kColSeg;      // 68 segments
+constexpr int64_t kNoAllocTotPitch = ((kNoAllocMaxW + 1 + 31) / 32) * 32;        // 3872 columns
+constexpr size_t kNoAllocJobBytes = 256;
+constexpr size_t kNoAllocTotS = static_cast<size_t>(kNoAllocTotRows * kNoAllocTotPitch) * sizeof(uint32_t);
+constexpr size_t kNoAllocTotQ = static_cast<size_t>(kNoAllocTotRows * kNoAllocTotPitch) * sizeof(uint64_t);
+constexpr size_t kNoAllocBytes = kNoAllocJobBytes + kNoAllocTotQ + kNoAllocTotS;
+static_assert(sizeof(IIJob) <= kNoAllocJobBytes, "job descriptor fits its slot");
+
+// Layout: [job descriptor | squared-sum totals | sum totals].
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// The job descriptor travels as a kernel parameter, so no host buffer has to
+// outlive the call.
+__global__ void store_job_kernel(IIJob* dst, IIJob job) { *dst = job; }
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (looked up once
+// per device, with that device current).
+int noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    VJ_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(VJ_RUNTIME_ERROR, "vj_integral_image_noalloc: device id");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return set_error(VJ_CUDA_ERROR, std::string("vj_integral_image_noalloc: cudaGetSymbolAddress: ") +
+                                                cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return VJ_OK;
+}
+
+}  // namespace
 }  // namespace vjgb
 
 using namespace vjgb;
 
 extern "C" {
+
+int vj_integral_image_noalloc(const uint8_t* d_gray, int w, int h, int stride, uint32_t* d_sum, uint64_t* d_sqsum,
+                              void* stream) {
+    if (!d_gray || !d_sum || !d_sqsum || w <= 0 || h <= 0 || stride < w)
+        return set_error(VJ_INVALID_ARG, "vj_integral_image_noalloc: bad arguments (d_sqsum is required)");
+    if (w > kNoAllocMaxW || h > kNoAllocMaxH)
+        return set_error(VJ_INVALID_ARG, "vj_integral_image_noalloc: image larger than 3840 x 2160, the size its "
+                                         "fixed scratch holds; use vj_integral_image");
+    unsigned char* base = nullptr;
+    const int st0 = noalloc_scratch(&base);
+    if (st0 != VJ_OK) return st0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    IIJob job{};
+    job.pix = d_gray;
+    job.stride = stride;
+    job.sum = d_sum;
+    job.sq = d_sqsum;
+    job.w = w;
+    job.h = h;
+    job.pitch = w + 1;
+    const IIPlan plan = plan_integral_jobs(&job, 1);
+    IIJob* d_job = reinterpret_cast<IIJob*>(base);
+    uint64_t* totQ = reinterpret_cast<uint64_t*>(base + kNoAllocJobBytes);
+    uint32_t* totS = reinterpret_cast<uint32_t*>(base + kNoAllocJobBytes + kNoAllocTotQ);
+    // Every total the column passes read is written first by col_total_kernel
+    // in the same call, so nothing left by an earlier call is ever read.
+    VJ_TIMED_LAUNCH("store_job_kernel", s, store_job_kernel<<<1, 1, 0, s>>>(d_job, job));
+    VJ_LAUNCH_CHECK("store_job_kernel");
+    const int st = launch_integral_jobs(d_job, 1, plan, totS, totQ, s);
+    return st == VJ_OK ? ok() : st;
+}
 
 int vj_integral_batch(const uint8_t* d_gray, int w, int h, int stride, int n, uint32_t* d_sumT,
                       uint64_t* d_sqsumT, float* d_invNorm, void* stream) {

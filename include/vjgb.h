@@ -198,6 +198,24 @@ int vj_integral_batch(const uint8_t* d_gray, int w, int h, int stride, int n,
 int vj_integral_image(const uint8_t* d_gray, int w, int h, int stride,
                       uint32_t* d_sum, uint64_t* d_sqsum, void* stream);
 
+/* vj_integral_image for callers that must not allocate device memory (no
+ * counterpart in the reference).  Some callers cannot call cudaMalloc: code
+ * running under a caller-owned memory pool or a fixed device-memory budget,
+ * and code that must not trigger the implicit synchronisation or the failure
+ * paths of the CUDA allocator in the middle of a latency-bound pipeline.
+ * This variant allocates nothing: its scratch (the column-pass segment totals
+ * and the job descriptor, about 3.2 MB) is a fixed array in device memory that
+ * every GPU loading the library holds until the process exits.  Limits:
+ * w <= 3840, h <= 2160, and d_sqsum must be given (there is no room for
+ * temporary squared sums); larger inputs return VJ_INVALID_ARG.  The first
+ * call on each device looks up the array's device address (cudaGetSymbolAddress),
+ * so make that first call before any stream capture.  Every call shares the
+ * one array: calls that overlap on the GPU (different streams, or different
+ * host threads) race and corrupt each other's results; keep them on one
+ * stream.  Asynchronous on `stream`; results equal vj_integral_image's. */
+int vj_integral_image_noalloc(const uint8_t* d_gray, int w, int h, int stride,
+                              uint32_t* d_sum, uint64_t* d_sqsum, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* AdaBoost stump search (vj::AdaBoostTrainer)                              */
 /* ------------------------------------------------------------------------ */
