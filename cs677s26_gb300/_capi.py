@@ -73,6 +73,7 @@ SIGNATURES = {
     "vj_stump_search": (i32, [vp, vp, vp, vp]),
     "vj_trainer_prepare_stage": (i32, [vp, vp]),
     "vj_trainer_stage_bytes": (i32, [vp, i32, pi64]),
+    "vj_trainer_last_round": (i32, [vp, vp]),
     "vj_round_update": (i32, [vp, vp, vp, vp, vp, vp]),
     "vj_stage_calibrate": (i32, [vp, vp, i32, f32, f32, i32, vp, vp]),
     "vj_detector_create": (i32, [i32, i32, i32, i32, i32, C.POINTER(vp)]),

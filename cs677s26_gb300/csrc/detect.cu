@@ -15,8 +15,8 @@
 //      stages and compacts the surviving windows with warp ballots between
 //      stages;
 //   4. queue passes: the survivors of the early stages from all tiles are
-//      processed densely, 32 windows per warp, a few stages per pass, with
-//      ballot compaction into the next queue;
+//      taken 256 at a time per warp and run through the next group of
+//      stages the same way, so deep stages also run on full warps;
 //   5. the survivors of the last stage become Detection records; the host
 //      sorts them into the reference CPU path's order (level, y, x),
 //      truncates to maxDetections and groups them (groupRectangles,
@@ -168,76 +168,95 @@ __device__ __forceinline__ float window_inv(const CasLevel& L, int x, int y, int
     return inv;
 }
 
-// Sum of one stage's stumps for the window at level offset `b`.
-__device__ __forceinline__ float stage_sum(const DStump* __restrict__ stumps, const DStage& st, const uint32_t* __restrict__ sum,
-                                           int64_t P, int64_t b, float inv) {
-    float acc = 0.0f;
-    for (int k = 0; k < st.ntrees; ++k) {
-        const DStump* sp = stumps + st.first + k;
-        const float4 a = __ldg(reinterpret_cast<const float4*>(sp));
-        const float4 wv = __ldg(reinterpret_cast<const float4*>(sp) + 1);
-        const int4 d = __ldg(reinterpret_cast<const int4*>(sp) + 2);
-        const int4 e = __ldg(reinterpret_cast<const int4*>(sp) + 3);
-        const int nr = __float_as_int(a.w);
-        const uint32_t dxw[3] = {static_cast<uint32_t>(d.x), static_cast<uint32_t>(d.y), static_cast<uint32_t>(d.z)};
-        const uint32_t dyw[3] = {static_cast<uint32_t>(d.w), static_cast<uint32_t>(e.x), static_cast<uint32_t>(e.y)};
-        const float wr[3] = {wv.x, wv.y, wv.z};
-        float raw = 0.0f;
+// Value of one stump (leftVal or rightVal) for the window at level offset `b`
+// (main.cu:785-797, face_vision_engine.cu:500-537).
+__device__ __forceinline__ float stump_value(const DStump* __restrict__ sp, const uint32_t* __restrict__ sum, int64_t P,
+                                             int64_t b, float inv) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(sp));
+    const float4 wv = __ldg(reinterpret_cast<const float4*>(sp) + 1);
+    const int4 d = __ldg(reinterpret_cast<const int4*>(sp) + 2);
+    const int4 e = __ldg(reinterpret_cast<const int4*>(sp) + 3);
+    const int nr = __float_as_int(a.w);
+    const uint32_t dxw[3] = {static_cast<uint32_t>(d.x), static_cast<uint32_t>(d.y), static_cast<uint32_t>(d.z)};
+    const uint32_t dyw[3] = {static_cast<uint32_t>(d.w), static_cast<uint32_t>(e.x), static_cast<uint32_t>(e.y)};
+    const float wr[3] = {wv.x, wv.y, wv.z};
+    float raw = 0.0f;
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            if (r < nr) {
-                float c[4];
+    for (int r = 0; r < 3; ++r) {
+        if (r < nr) {
+            float c[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int ci = 4 * r + q;
-                    const int dx = static_cast<int8_t>((dxw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
-                    const int dy = static_cast<int8_t>((dyw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
-                    c[q] = corner_f(__ldg(sum + b + dy * P + dx));
-                }
-                const float v = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(c[0], c[1]), c[2]), c[3]), wr[r]);
-                raw = (r == 0) ? v : __fadd_rn(raw, v);
+            for (int q = 0; q < 4; ++q) {
+                const int ci = 4 * r + q;
+                const int dx = static_cast<int8_t>((dxw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
+                const int dy = static_cast<int8_t>((dyw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
+                c[q] = corner_f(__ldg(sum + b + dy * P + dx));
             }
+            const float v = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(c[0], c[1]), c[2]), c[3]), wr[r]);
+            raw = (r == 0) ? v : __fadd_rn(raw, v);
         }
-        const float resp = __fmul_rn(raw, inv);
-        acc = __fadd_rn(acc, resp < a.x ? a.y : a.z);
     }
+    return __fmul_rn(raw, inv) < a.x ? a.y : a.z;
+}
+
+// Sum of one stage's stumps, added in stump order.  Four stumps are
+// evaluated before their values are added so their ~40 integral loads are in
+// flight together; the additions keep the reference's order, so the sum is
+// the same float.
+__device__ __forceinline__ float stage_sum(const DStump* __restrict__ stumps, const DStage& st,
+                                           const uint32_t* __restrict__ sum, int64_t P, int64_t b, float inv) {
+    const DStump* sp = stumps + st.first;
+    float acc = 0.0f;
+    int k = 0;
+    for (; k + 4 <= st.ntrees; k += 4) {
+        const float c0 = stump_value(sp + k, sum, P, b, inv);
+        const float c1 = stump_value(sp + k + 1, sum, P, b, inv);
+        const float c2 = stump_value(sp + k + 2, sum, P, b, inv);
+        const float c3 = stump_value(sp + k + 3, sum, P, b, inv);
+        acc = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(acc, c0), c1), c2), c3);
+    }
+    for (; k < st.ntrees; ++k) acc = __fadd_rn(acc, stump_value(sp + k, sum, P, b, inv));
     return acc;
 }
 
-__device__ __forceinline__ void emit(const CasLevel& L, int x, int y, int winW, int winH, float score,
+__device__ __forceinline__ void emit(const CasLevel* __restrict__ levels, const QEntry& e, int winW, int winH,
                                      vj_detection* __restrict__ out, int cap, int* __restrict__ counts, bool valid) {
     const unsigned m = __ballot_sync(0xffffffffu, valid);
     if (!m) return;
     const int lane = threadIdx.x & 31;
-    // One atomic per (warp, image): lanes of one warp all belong to the same
-    // image only in the tile pass; in the queue passes they may not.
-    const unsigned peers = __match_any_sync(0xffffffffu, valid ? L.image : -1);
+    const int image = valid ? __ldg(&levels[e.level].image) : -1;
+    // one atomic per image present in the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, image);
     int base = 0;
     const int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) base = atomicAdd(counts + L.image, __popc(peers));
+    if (valid && lane == leader) base = atomicAdd(counts + image, __popc(peers));
     base = __shfl_sync(0xffffffffu, base, leader);
     if (!valid) return;
     const int slot = base + __popc(peers & lanemask_lt());
     if (slot < cap) {
+        const float scale = __ldg(&levels[e.level].scale);
+        const int x = static_cast<int>(e.xy & 0xFFFFu), y = static_cast<int>(e.xy >> 16);
         vj_detection d;
-        d.x = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(x), L.scale), 0.5f));
-        d.y = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(y), L.scale), 0.5f));
-        d.w = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(winW), L.scale), 0.5f));
-        d.h = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(winH), L.scale), 0.5f));
-        d.scaleIdx = L.scaleIdx;
-        d.score = score;
-        out[static_cast<size_t>(L.image) * cap + slot] = d;
+        d.x = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(x), scale), 0.5f));
+        d.y = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(y), scale), 0.5f));
+        d.w = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(winW), scale), 0.5f));
+        d.h = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(winH), scale), 0.5f));
+        d.scaleIdx = __ldg(&levels[e.level].scaleIdx);
+        d.score = e.score;
+        out[static_cast<size_t>(image) * cap + slot] = d;
     }
 }
 
 struct CasArgs {
     const CasLevel* levels;
     int nLevels;
-    int64_t totalTiles;
+    int64_t totalTiles;   // windows come from tiles of the levels when qin is null
+    const QEntry* qin;    // otherwise from this queue
+    const int* qinCount;
+    int qinCap;
     const DStump* stumps;
     const DStage* stages;
-    int stageEnd;   // tile pass runs stages [0, stageEnd)
-    int nStages;
+    int s0, s1, nStages;  // this pass runs stages [s0, s1)
     int winW, winH, normMode;
     unsigned long long* workCounter;
     QEntry* qout;
@@ -257,7 +276,8 @@ __device__ __forceinline__ int find_level(const CasLevel* __restrict__ levels, i
     return lo;
 }
 
-// Appends `valid` lanes' entries to a queue with one atomic per warp.
+// Appends `valid` lanes' entries to a queue with one atomic per warp; the
+// counter keeps counting past qcap so the host sees an overflow.
 __device__ __forceinline__ void push_queue(QEntry* __restrict__ q, int* __restrict__ qcount, int qcap, bool valid,
                                            const QEntry& e) {
     const unsigned m = __ballot_sync(0xffffffffu, valid);
@@ -272,140 +292,98 @@ __device__ __forceinline__ void push_queue(QEntry* __restrict__ q, int* __restri
     }
 }
 
-// Tile pass: variance gate + stages [0, stageEnd) with ballot compaction.
+constexpr int kListCap = kTileW * kTileH;  // windows a warp holds at once
+
+// One cascade pass.  Each warp repeatedly takes a batch of windows - a 32x8
+// tile of some level (after the variance gate), or up to 256 queue entries -
+// into a private list in shared memory, runs stages [s0, s1) over it 32
+// windows at a time, and after every stage compacts the survivors with a
+// ballot so the next stage again runs on full warps.  Survivors go to the
+// next queue, or become detections after the last stage.
 __global__ void __launch_bounds__(kCasWarps * 32)
-cascade_tile_kernel(CasArgs A) {
-    __shared__ uint16_t lst[kCasWarps][kTileW * kTileH];
-    __shared__ float linv[kCasWarps][kTileW * kTileH];
-    __shared__ float lsc[kCasWarps][kTileW * kTileH];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint16_t* L_ = lst[w];
-    float* I_ = linv[w];
-    float* S_ = lsc[w];
+cascade_kernel(CasArgs A) {
+    __shared__ QEntry lst[kCasWarps][kListCap];
+    const int lane = threadIdx.x & 31;
+    QEntry* Lst = lst[threadIdx.x >> 5];
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(A.workCounter, 1ull);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= static_cast<unsigned long long>(A.totalTiles)) break;
-        const CasLevel L = A.levels[find_level(A.levels, A.nLevels, static_cast<int64_t>(t))];
-        const int64_t local = static_cast<int64_t>(t) - L.tileBase;
-        const int tx = static_cast<int>(local % L.tilesX), ty = static_cast<int>(local / L.tilesX);
         int count = 0;
-        for (int r = 0; r < kTileH; ++r) {
-            const int gx = tx * kTileW + lane, gy = ty * kTileH + r;
-            float iv = 0.0f;
-            if (gx < L.scanW && gy < L.scanH) iv = window_inv(L, gx * L.step, gy * L.step, A.winW, A.winH, A.normMode);
-            const bool ok = iv != 0.0f;
-            const unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) {
-                const int pos = count + __popc(m & lanemask_lt());
-                L_[pos] = static_cast<uint16_t>(r * kTileW + lane);
-                I_[pos] = iv;
+        if (A.qin == nullptr) {
+            if (t >= static_cast<unsigned long long>(A.totalTiles)) break;
+            const int li = find_level(A.levels, A.nLevels, static_cast<int64_t>(t));
+            const CasLevel L = A.levels[li];
+            const int64_t local = static_cast<int64_t>(t) - L.tileBase;
+            const int tx = static_cast<int>(local % L.tilesX), ty = static_cast<int>(local / L.tilesX);
+            for (int r = 0; r < kTileH; ++r) {
+                const int gx = tx * kTileW + lane, gy = ty * kTileH + r;
+                const int x = gx * L.step, y = gy * L.step;
+                float iv = 0.0f;
+                if (gx < L.scanW && gy < L.scanH) iv = window_inv(L, x, y, A.winW, A.winH, A.normMode);
+                const bool ok = iv != 0.0f;
+                const unsigned m = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    QEntry e;
+                    e.level = static_cast<uint32_t>(li);
+                    e.xy = (static_cast<uint32_t>(y) << 16) | static_cast<uint32_t>(x);
+                    e.inv = iv;
+                    e.score = 0.0f;
+                    Lst[count + __popc(m & lanemask_lt())] = e;
+                }
+                count += __popc(m);
             }
-            count += __popc(m);
+        } else {
+            // Entries per warp: enough to keep every warp of the grid busy,
+            // between 32 and the list capacity.
+            const int n = min(*A.qinCount, A.qinCap);
+            const int warps = gridDim.x * kCasWarps;
+            const int chunk = min(kListCap, max(32, ((n + warps - 1) / warps + 31) & ~31));
+            const int64_t base = static_cast<int64_t>(t) * chunk;
+            if (base >= n) break;
+            count = static_cast<int>(n - base < chunk ? n - base : chunk);
+            for (int i = lane; i < count; i += 32) Lst[i] = A.qin[base + i];
         }
         __syncwarp();
-        for (int si = 0; si < A.stageEnd && count > 0; ++si) {
+        for (int si = A.s0; si < A.s1 && count > 0; ++si) {
             const DStage st = A.stages[si];
             int nc = 0;
             for (int g = 0; g < count; g += 32) {
                 const int i = g + lane;
                 const bool act = i < count;
-                int id = 0;
-                float iv = 0.0f, s = 0.0f;
+                QEntry e{};
+                float s = 0.0f;
                 if (act) {
-                    id = L_[i];
-                    iv = I_[i];
-                    const int x = (tx * kTileW + (id & 31)) * L.step, y = (ty * kTileH + (id >> 5)) * L.step;
-                    s = stage_sum(A.stumps, st, L.sum, L.pitch, static_cast<int64_t>(y) * L.pitch + x, iv);
+                    e = Lst[i];
+                    const CasLevel* L = A.levels + e.level;
+                    const int64_t P = __ldg(&L->pitch);
+                    const uint32_t* sum = reinterpret_cast<const uint32_t*>(__ldg(reinterpret_cast<const unsigned long long*>(&L->sum)));
+                    const int64_t b = static_cast<int64_t>(e.xy >> 16) * P + static_cast<int64_t>(e.xy & 0xFFFFu);
+                    s = stage_sum(A.stumps, st, sum, P, b, e.inv);
                 }
                 const bool pass = act && !(s < st.threshold);
                 const unsigned m = __ballot_sync(0xffffffffu, pass);
                 __syncwarp();
                 if (pass) {
-                    const int pos = nc + __popc(m & lanemask_lt());
-                    L_[pos] = static_cast<uint16_t>(id);
-                    I_[pos] = iv;
-                    S_[pos] = s;
+                    e.score = s;
+                    Lst[nc + __popc(m & lanemask_lt())] = e;
                 }
                 nc += __popc(m);
                 __syncwarp();
             }
             count = nc;
         }
-        // Survivors leave the tile: to the queue, or out as detections.
         for (int g = 0; g < count; g += 32) {
             const int i = g + lane;
             const bool act = i < count;
-            int x = 0, y = 0;
             QEntry e{};
-            if (act) {
-                const int id = L_[i];
-                x = (tx * kTileW + (id & 31)) * L.step;
-                y = (ty * kTileH + (id >> 5)) * L.step;
-                e.level = static_cast<uint32_t>(find_level(A.levels, A.nLevels, static_cast<int64_t>(t)));
-                e.xy = (static_cast<uint32_t>(y) << 16) | static_cast<uint32_t>(x);
-                e.inv = I_[i];
-                e.score = S_[i];
-            }
-            if (A.stageEnd >= A.nStages)
-                emit(L, x, y, A.winW, A.winH, e.score, A.dets, A.detCap, A.detCounts, act);
+            if (act) e = Lst[i];
+            if (A.s1 >= A.nStages)
+                emit(A.levels, e, A.winW, A.winH, A.dets, A.detCap, A.detCounts, act);
             else
                 push_queue(A.qout, A.qoutCount, A.qcap, act, e);
         }
         __syncwarp();
-    }
-}
-
-struct QArgs {
-    const CasLevel* levels;
-    const DStump* stumps;
-    const DStage* stages;
-    int s0, s1, nStages;
-    int winW, winH;
-    const QEntry* qin;
-    const int* qinCount;
-    int qinCap;
-    QEntry* qout;
-    int* qoutCount;
-    int qcap;
-    vj_detection* dets;
-    int detCap;
-    int* detCounts;
-};
-
-// Queue pass: stages [s0, s1) on dense groups of 32 windows.
-__global__ void __launch_bounds__(256)
-cascade_queue_kernel(QArgs A) {
-    const int n = min(*A.qinCount, A.qinCap);
-    const int64_t nthreads = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t base = static_cast<int64_t>(blockIdx.x) * blockDim.x; base < n; base += nthreads) {
-        const int64_t i = base + threadIdx.x;
-        const bool act = i < n;
-        QEntry e{};
-        CasLevel L{};
-        bool pass = false;
-        if (act) {
-            e = A.qin[i];
-            L = A.levels[e.level];
-            const int x = static_cast<int>(e.xy & 0xFFFFu), y = static_cast<int>(e.xy >> 16);
-            const int64_t b = static_cast<int64_t>(y) * L.pitch + x;
-            pass = true;
-            for (int si = A.s0; si < A.s1; ++si) {
-                const DStage st = A.stages[si];
-                const float s = stage_sum(A.stumps, st, L.sum, L.pitch, b, e.inv);
-                if (s < st.threshold) {
-                    pass = false;
-                    break;
-                }
-                e.score = s;
-            }
-        }
-        if (A.s1 >= A.nStages)
-            emit(L, static_cast<int>(e.xy & 0xFFFFu), static_cast<int>(e.xy >> 16), A.winW, A.winH, e.score, A.dets,
-                 A.detCap, A.detCounts, pass);
-        else
-            push_queue(A.qout, A.qoutCount, A.qcap, pass, e);
     }
 }
 
@@ -642,23 +620,32 @@ struct vj_detector {
     // Work buffers, grown on demand.
     DBuf imgs, pix, iiSum, iiSq, totS, totQ, plan, qA, qB, dets, counts, ctrs;
     HBuf hplan, hcounts, hdets;
-    // Stage schedule: tile pass covers [0, tileStages); queue passes follow.
+    // Stage schedule: the tile pass covers [0, tileStages); queue passes end
+    // at passEnds.  Capacity hints carry the largest queue and per-image raw
+    // detection counts seen so far, so a repeat workload needs no retry.
     int tileStages = 0;
     std::vector<int> passEnds;
+    int tileStumps = 64, passStumps = 600;
+    int64_t qHint = 0;
+    int detHint = 0;
 };
 
 namespace {
 
-// The autotunable schedule: tile pass until ~128 stumps, then passes of at
-// least 160 stumps each; the last pass takes the rest.
+// Stage schedule: the tile pass runs stages until it has covered tileStumps
+// stumps; each queue pass then covers at least passStumps stumps (the last
+// takes the rest).  At most 7 queue passes (work counters available).
 void schedule_passes(vj_detector* d) {
     int acc = 0, s = 0;
-    while (s < d->nStages && (acc < 128 || s == 0)) acc += d->hStages[s++].ntrees;
+    while (s < d->nStages && (acc < d->tileStumps || s == 0)) acc += d->hStages[s++].ntrees;
     d->tileStages = s;
     d->passEnds.clear();
+    int remaining = 0;
+    for (int k = s; k < d->nStages; ++k) remaining += d->hStages[k].ntrees;
+    const int per = std::max(d->passStumps, (remaining + 6) / 7);
     while (s < d->nStages) {
         int a = 0;
-        while (s < d->nStages && a < 160) a += d->hStages[s++].ntrees;
+        while (s < d->nStages && a < per) a += d->hStages[s++].ntrees;
         d->passEnds.push_back(s);
     }
 }
@@ -766,8 +753,9 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
     // Queue and raw-detection capacities start from typical occupancy; the
     // counters keep counting past capacity, so an overflow is detected and the
     // call repeated with the sizes it needed.
-    int qcap = static_cast<int>(std::min<int64_t>(std::max<int64_t>(windows / 8, 1 << 16), INT32_MAX / 2));
-    int detCap = std::max(64, std::min(D->maxDet, 4096));
+    int qcap = static_cast<int>(
+        std::min<int64_t>(std::max<int64_t>({windows / 8, int64_t(1) << 16, D->qHint}), INT32_MAX / 2));
+    int detCap = std::max({64, std::min(D->maxDet, 4096), D->detHint});
     // ---- plan upload: [IIJob][CasLevel][ResizeJob...]
     std::vector<int64_t> rjOff;
     int64_t planBytes = align_up(sizeof(IIJob) * iij.size(), 64);
@@ -820,57 +808,54 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
         VJ_CUDA_TRY(cudaMemsetAsync(D->ctrs.p, 0, 64, s));
         int* qCount = D->counts.as<int>() + nImg;  // two queue counters after the image counts
         const CasLevel* dLv = reinterpret_cast<const CasLevel*>(dp + lvOff);
+        unsigned long long* ctr = D->ctrs.as<unsigned long long>();  // one work counter per pass
         CasArgs ca{};
         ca.levels = dLv;
         ca.nLevels = static_cast<int>(lv.size());
         ca.totalTiles = tiles;
+        ca.qin = nullptr;
         ca.stumps = D->stumps.as<DStump>();
         ca.stages = D->stages.as<DStage>();
-        ca.stageEnd = D->tileStages;
+        ca.s0 = 0;
+        ca.s1 = D->tileStages;
         ca.nStages = D->nStages;
         ca.winW = D->winW;
         ca.winH = D->winH;
         ca.normMode = D->normMode;
-        ca.workCounter = D->ctrs.as<unsigned long long>();
+        ca.workCounter = ctr;
         ca.qout = D->qA.as<QEntry>();
         ca.qoutCount = qCount;
         ca.qcap = qcap;
         ca.dets = D->dets.as<vj_detection>();
         ca.detCap = detCap;
         ca.detCounts = D->counts.as<int>();
+        const int casGrid = sm_count_d() * 8;
+        static const char* const kPassName[8] = {"cascade_kernel(tiles)", "cascade_kernel(pass1)",
+                                                 "cascade_kernel(pass2)", "cascade_kernel(pass3)",
+                                                 "cascade_kernel(pass4)", "cascade_kernel(pass5)",
+                                                 "cascade_kernel(pass6)", "cascade_kernel(pass7)"};
         if (tiles > 0) {
-            VJ_TIMED_LAUNCH("cascade_tile_kernel", s,
-                            cascade_tile_kernel<<<sm_count_d() * 8, kCasWarps * 32, 0, s>>>(ca));
-            VJ_LAUNCH_CHECK("cascade_tile_kernel");
+            VJ_TIMED_LAUNCH(kPassName[0], s, cascade_kernel<<<casGrid, kCasWarps * 32, 0, s>>>(ca));
+            VJ_LAUNCH_CHECK("cascade_kernel");
         }
-        int s0 = D->tileStages;
         QEntry* qin = D->qA.as<QEntry>();
         QEntry* qout = D->qB.as<QEntry>();
         int* cin = qCount;
         int* cout = qCount + 1;
         for (size_t p = 0; p < D->passEnds.size(); ++p) {
             VJ_CUDA_TRY(cudaMemsetAsync(cout, 0, sizeof(int), s));
-            QArgs qa{};
-            qa.levels = dLv;
-            qa.stumps = ca.stumps;
-            qa.stages = ca.stages;
-            qa.s0 = s0;
-            qa.s1 = D->passEnds[p];
-            qa.nStages = D->nStages;
-            qa.winW = D->winW;
-            qa.winH = D->winH;
+            CasArgs qa = ca;
             qa.qin = qin;
             qa.qinCount = cin;
             qa.qinCap = qcap;
+            qa.s0 = p == 0 ? D->tileStages : D->passEnds[p - 1];
+            qa.s1 = D->passEnds[p];
+            qa.workCounter = ctr + 1 + p;
             qa.qout = qout;
             qa.qoutCount = cout;
-            qa.qcap = qcap;
-            qa.dets = ca.dets;
-            qa.detCap = detCap;
-            qa.detCounts = ca.detCounts;
-            VJ_TIMED_LAUNCH("cascade_queue_kernel", s, cascade_queue_kernel<<<sm_count_d() * 8, 256, 0, s>>>(qa));
-            VJ_LAUNCH_CHECK("cascade_queue_kernel");
-            s0 = D->passEnds[p];
+            VJ_TIMED_LAUNCH(kPassName[std::min<size_t>(p + 1, 7)], s,
+                            cascade_kernel<<<casGrid, kCasWarps * 32, 0, s>>>(qa));
+            VJ_LAUNCH_CHECK("cascade_kernel");
             std::swap(qin, qout);
             std::swap(cin, cout);
         }
@@ -880,6 +865,8 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
         int need = 0, qneed = 0;
         for (int i = 0; i < nImg; ++i) need = std::max(need, hc[i]);
         qneed = std::max(hc[nImg], hc[nImg + 1]);
+        D->qHint = std::max<int64_t>(D->qHint, qneed + qneed / 4);
+        D->detHint = std::max(D->detHint, need + need / 4);
         if (qneed > qcap || need > detCap) {
             qcap = std::max(qcap, qneed);
             detCap = std::max(detCap, need);

@@ -11,8 +11,8 @@
 // Design here:
 //   1. eval_sort_kernel: one CTA per feature evaluates the exact normalised
 //      responses of all samples into shared memory and sorts them with an
-//      on-chip stable LSD radix sort (4 x 8-bit digits, warp match-any ranking,
-//      per-warp digit counters).  It writes the sorted sample order (2 B per
+//      on-chip stable LSD radix sort (4 x 8-bit digits, ranks from warp
+//      ballots, per-warp digit counters).  It writes the sorted sample order (2 B per
 //      feature-sample) and a bitmask of valid split positions
 //      (v[k] + 1e-7f < v[k+1], boosting_core.cu:400).
 //   2. sweep_kernel: one warp per feature streams that order, gathers signed
@@ -45,6 +45,8 @@ constexpr int kCntStride = 33;  // per-digit row of 32 warp counters, padded aga
 constexpr int kSweepThreads = 512;
 constexpr int kSweepWarps = kSweepThreads / 32;
 constexpr int kSmemWeightsMax = 49152;  // samples whose weights fit in shared memory
+constexpr int kRefineThreads = 256;
+constexpr int kRefineWarps = kRefineThreads / 32;
 constexpr float kU = 5.9604645e-08f;    // 2^-24, unit roundoff of FP32
 
 struct RoundParams {
@@ -88,9 +90,19 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
         } else {
             if (tid == 0) sfeat = feats[featBegin + fl];
             __syncthreads();
-            const vj_haar_feature f = sfeat;
-            for (int s = tid; s < n; s += kSortThreads)
-                keys[s] = __float_as_uint(train_response(f, sumT, n, s, __ldg(invNorm + s)));
+            const vj_haar_feature& f = sfeat;  // read from shared memory (broadcast), not held in registers
+            // four samples per iteration keep ~40 independent L2 loads in flight
+            for (int s0 = tid; s0 < n; s0 += 4 * kSortThreads) {
+                float r[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int s = s0 + u * kSortThreads;
+                    r[u] = s < n ? train_response(f, sumT, n, s, __ldg(invNorm + s)) : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (s0 + u * kSortThreads < n) keys[s0 + u * kSortThreads] = __float_as_uint(r[u]);
+            }
         }
         for (int p = tid; p < NP; p += kSortThreads) idx[p] = static_cast<uint16_t>(p);
         __syncthreads();
@@ -103,6 +115,8 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
             // (warp, j, lane) order is the current sequence order and ranks are
             // stable.  The leader of each equal-digit group bumps the warp's
             // counter for that digit.
+            // Digits first (independent loads), then ranks: peers with the
+            // same digit in a step come from 8 ballots, one per digit bit.
             uint32_t packed[R];
             uint32_t dig[(R + 3) / 4];
 #pragma unroll
@@ -110,7 +124,21 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                 const int p = warp * 32 * R + j * 32 + lane;
                 const uint32_t id = idx[p];
                 const uint32_t d = id < static_cast<uint32_t>(n) ? (radix_key(keys[id]) >> shift) & 255u : 255u;
-                const uint32_t peers = __match_any_sync(0xffffffffu, d);
+                packed[j] = id;
+                if ((j & 3) == 0)
+                    dig[j >> 2] = d;
+                else
+                    dig[j >> 2] |= d << (8 * (j & 3));
+            }
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                const uint32_t d = (dig[j >> 2] >> (8 * (j & 3))) & 255u;
+                uint32_t peers = 0xffffffffu;
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const uint32_t m = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+                    peers &= ((d >> b) & 1u) ? m : ~m;
+                }
                 const int leader = __ffs(peers) - 1;
                 uint32_t old = 0;
                 if (lane == leader) {
@@ -118,11 +146,7 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                     cnt[d * kCntStride + warp] = old + __popc(peers);
                 }
                 old = __shfl_sync(0xffffffffu, old, leader);
-                packed[j] = id | ((old + __popc(peers & lanemask_lt())) << 16);
-                if ((j & 3) == 0)
-                    dig[j >> 2] = d;
-                else
-                    dig[j >> 2] |= d << (8 * (j & 3));
+                packed[j] |= (old + __popc(peers & lanemask_lt())) << 16;
             }
             __syncthreads();
             // Exclusive scan of the counters in (digit, warp) order.
@@ -286,86 +310,127 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t
         __syncthreads();
         wsg = wsgS;
     }
-    const float TP = prm->tp, W = prm->w;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // With P(k) the prefix sum of signed weights over the sorted order, the
+    // two parities' errors at split k are T+ - P(k) and T- + P(k), so a
+    // feature's best error is min(T+ - max P, T- + min P) over valid splits.
+    //
+    // Each warp walks the flattened sequence of (feature, chunk) items of the
+    // features it owns; a chunk is 512 positions, 16 per lane (two 16-byte
+    // index loads + 16 split bits).  The loads of the next item are issued
+    // before the current one is processed, across feature boundaries, so each
+    // warp keeps two chunks of index traffic in flight.
+    const float TP = prm->tp, TN = prm->tn;
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
+    const int nw = gridDim.x * kSweepWarps;
+    const int cpf = (n - 1 + 511) / 512;                     // chunks per feature (split positions 0..n-2)
+    const int myFeat = gw < featCount ? (featCount - gw + nw - 1) / nw : 0;
+    const int items = myFeat * cpf;
+    // (f, c): feature and chunk of the item to load next.  Used features are
+    // streamed like the others and dropped at the end, so no load waits on
+    // the mask.
+    auto load = [&](int it, int f, int c, uint4& a, uint4& b, uint32_t& g) {
+        a = b = make_uint4(0, 0, 0, 0);
+        g = 0;
+        if (it >= items) return;
+        const int k0 = c * 512 + lane * 16;
+        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
+        if (k0 < n) a = __ldg(reinterpret_cast<const uint4*>(row + k0));
+        if (k0 + 8 < n) b = __ldg(reinterpret_cast<const uint4*>(row + k0 + 8));
+        if (k0 < n - 1) g = (__ldg(gap + static_cast<size_t>(f) * gapStride + (k0 >> 5)) >> (k0 & 31)) & 0xFFFFu;
+    };
     float blockMin = INFINITY;
-    for (int f = blockIdx.x * kSweepWarps + warp; f < featCount; f += gridDim.x * kSweepWarps) {
-        float best = INFINITY;
-        if (!(usedMask && usedMask[f])) {
-            const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
-            const uint32_t* grow = gap + static_cast<size_t>(f) * gapStride;
-            float cp = 0.0f, cn = 0.0f, kp = 0.0f, kn = 0.0f;
-            for (int base = 0; base < n - 1; base += 256) {
-                const int k0 = base + lane * 8;
-                uint4 v = make_uint4(0, 0, 0, 0);
-                uint32_t g = 0;
-                if (k0 < n) v = __ldg(reinterpret_cast<const uint4*>(row + k0));
-                if (k0 < n - 1) g = (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu;
-                const uint32_t ids[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
-                                         v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
-                float lp[8], ln[8];
-                float sp = 0.0f, sn = 0.0f;
+    uint4 ca, cb;
+    uint32_t cg;
+    int f = gw, c = 0;        // item being processed
+    int fn = gw, cn = 1;      // item being loaded
+    if (cn == cpf) {
+        cn = 0;
+        fn += nw;
+    }
+    load(0, f, c, ca, cb, cg);
+    float carry = 0.0f, comp = 0.0f, pmin = INFINITY, pmax = -INFINITY;
+    for (int it = 0; it < items; ++it) {
+        uint4 na, nb;
+        uint32_t ng;
+        load(it + 1, fn, cn, na, nb, ng);
+        if (++cn == cpf) {
+            cn = 0;
+            fn += nw;
+        }
+        const int k0 = c * 512 + lane * 16;
+        const uint32_t w8[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+        // Lane-local running prefix s; its minimum and maximum over the valid
+        // split positions.  Rounding is monotone, so min_i fl(b + s_i) equals
+        // fl(b + min_i s_i): the chunk base b is added once per lane.
+        float s = 0.0f, lmin = INFINITY, lmax = -INFINITY;
+        if (k0 + 16 <= n) {
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    // positions past n hold padding indices: read sample 0, add nothing
-                    const bool in = k0 + i < n;
-                    const float x = in ? wsg[in ? ids[i] : 0u] : 0.0f;
-                    sp = __fadd_rn(sp, fmaxf(x, 0.0f));
-                    sn = __fadd_rn(sn, fmaxf(-x, 0.0f));
-                    lp[i] = sp;
-                    ln[i] = sn;
-                }
-                float ip = sp, in = sn;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const float yp = __shfl_up_sync(0xffffffffu, ip, o);
-                    const float yn = __shfl_up_sync(0xffffffffu, in, o);
-                    if (lane >= o) {
-                        ip = __fadd_rn(ip, yp);
-                        in = __fadd_rn(in, yn);
-                    }
-                }
-                float ep = __shfl_up_sync(0xffffffffu, ip, 1);
-                float en = __shfl_up_sync(0xffffffffu, in, 1);
-                if (lane == 0) ep = en = 0.0f;
-                const float totp = __shfl_sync(0xffffffffu, ip, 31);
-                const float totn = __shfl_sync(0xffffffffu, in, 31);
-                const float bp = __fadd_rn(cp, ep), bn = __fadd_rn(cn, en);
-                if (g) {
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        if ((g >> i) & 1u) {
-                            const float Lp = __fadd_rn(bp, lp[i]);
-                            const float Ln = __fadd_rn(bn, ln[i]);
-                            const float eP = __fadd_rn(Ln, __fsub_rn(TP, Lp));
-                            const float eN = __fsub_rn(W, eP);
-                            best = fminf(best, fminf(eP, eN));
-                        }
-                    }
-                }
-                // Kahan-compensated carries across chunks.
-                {
-                    const float y = __fsub_rn(totp, kp);
-                    const float t = __fadd_rn(cp, y);
-                    kp = __fsub_rn(__fsub_rn(t, cp), y);
-                    cp = t;
-                }
-                {
-                    const float y = __fsub_rn(totn, kn);
-                    const float t = __fadd_rn(cn, y);
-                    kn = __fsub_rn(__fsub_rn(t, cn), y);
-                    cn = t;
+            for (int i = 0; i < 16; ++i) {
+                s = __fadd_rn(s, wsg[(w8[i >> 1] >> (16 * (i & 1))) & 0xFFFFu]);
+                if ((cg >> i) & 1u) {
+                    lmin = fminf(lmin, s);
+                    lmax = fmaxf(lmax, s);
                 }
             }
+        } else {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_xor_sync(0xffffffffu, best, o));
-            best = fmaxf(best, 0.0f);
+            for (int i = 0; i < 16; ++i) {
+                // positions past n hold padding indices: read sample 0, add nothing
+                const bool in = k0 + i < n;
+                const uint32_t id = in ? ((w8[i >> 1] >> (16 * (i & 1))) & 0xFFFFu) : 0u;
+                s = __fadd_rn(s, in ? wsg[id] : 0.0f);
+                if ((cg >> i) & 1u) {
+                    lmin = fminf(lmin, s);
+                    lmax = fmaxf(lmax, s);
+                }
+            }
         }
-        if (lane == 0) fastErr[f] = best;
-        blockMin = fminf(blockMin, best);
+        float incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl = __fadd_rn(incl, y);
+        }
+        float excl = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0) excl = 0.0f;
+        const float tot = __shfl_sync(0xffffffffu, incl, 31);
+        const float b0 = __fadd_rn(carry, excl);
+        if (lmax > -INFINITY) {
+            pmin = fminf(pmin, __fadd_rn(b0, lmin));
+            pmax = fmaxf(pmax, __fadd_rn(b0, lmax));
+        }
+        {
+            const float y = __fsub_rn(tot, comp);
+            const float t = __fadd_rn(carry, y);
+            comp = __fsub_rn(__fsub_rn(t, carry), y);
+            carry = t;
+        }
+        if (c == cpf - 1) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                pmin = fminf(pmin, __shfl_xor_sync(0xffffffffu, pmin, o));
+                pmax = fmaxf(pmax, __shfl_xor_sync(0xffffffffu, pmax, o));
+            }
+            float best = INFINITY;
+            if (pmax > -INFINITY && !(usedMask && usedMask[f]))
+                best = fmaxf(fminf(__fsub_rn(TP, pmax), __fadd_rn(TN, pmin)), 0.0f);
+            if (lane == 0) fastErr[f] = best;
+            blockMin = fminf(blockMin, best);
+            carry = comp = 0.0f;
+            pmin = INFINITY;
+            pmax = -INFINITY;
+        }
+        if (++c == cpf) {
+            c = 0;
+            f += nw;
+        }
+        ca = na;
+        cb = nb;
+        cg = ng;
     }
     __shared__ float wmin[kSweepWarps];
-    if (lane == 0) wmin[warp] = blockMin;
+    if (lane == 0) wmin[threadIdx.x >> 5] = blockMin;
     __syncthreads();
     if (threadIdx.x == 0) {
         float m = INFINITY;
@@ -393,78 +458,135 @@ __global__ void select_candidates_kernel(const float* __restrict__ fastErr, int 
 //    replaces parity -1).
 // ---------------------------------------------------------------------------
 template <bool kSmemW>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kRefineThreads)
 refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
               int64_t gapStride, const float* __restrict__ wsgG, int n, RoundParams* __restrict__ prm,
               const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit) {
     extern __shared__ float wsgS[];
+    __shared__ __align__(16) float stage[kRefineWarps][256];   // gathered weights of one chunk, in order
+    __shared__ __align__(16) float2 pre[kRefineWarps][256];    // (left positive, left negative) after each position
     const float* wsg = wsgG;
     if (kSmemW) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) wsgS[i] = wsgG[i];
         __syncthreads();
         wsg = wsgS;
     }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nc = prm->ncand;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    // One warp per candidate feature.  The warp streams the feature's sorted
+    // order 256 positions at a time (one coalesced 16-byte load per lane,
+    // issued a chunk ahead), gathers the signed weights into `stage` in
+    // order, and lane 0 replays the reference's sequential FP32 additions
+    // (main.cu:626-678) from there.  Inactive samples carry a zero weight and
+    // the accumulator of the other class adds +0.0f: both leave an FP32 sum
+    // of non-negative terms unchanged, exactly as skipping them does.
+    for (int c = blockIdx.x * kRefineWarps + w; c < nc; c += gridDim.x * kRefineWarps) {
         const int f = cand[c];
         const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
         const uint32_t* grow = gap + static_cast<size_t>(f) * gapStride;
-        float tp = 0.0f, tn = 0.0f;
-        for (int k0 = 0; k0 < n; k0 += 8) {
-            const uint4 v = __ldg(reinterpret_cast<const uint4*>(row + k0));
-            const uint32_t ids[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
-                                     v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+        auto load = [&](int base) {
+            const int k0 = base + lane * 8;
+            return (k0 < n) ? __ldg(reinterpret_cast<const uint4*>(row + k0)) : make_uint4(0, 0, 0, 0);
+        };
+        auto gather = [&](int base, const uint4& v) {
+            const int k0 = base + lane * 8;
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+            float x[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                if (k0 + i < n) {
-                    const float x = wsg[ids[i]];
-                    if (signbit(x))
-                        tn = __fadd_rn(tn, -x);
-                    else
-                        tp = __fadd_rn(tp, x);
-                }
+            for (int h = 0; h < 8; ++h) {
+                const bool in = k0 + h < n;
+                const uint32_t id = in ? ((w4[h >> 1] >> (16 * (h & 1))) & 0xFFFFu) : 0u;
+                x[h] = in ? wsg[id] : 0.0f;
             }
-        }
-        float lp = 0.0f, ln = 0.0f, bestErr = INFINITY;
-        int bestPar = 1, bestK = -1;
-        for (int k0 = 0; k0 < n - 1; k0 += 8) {
-            const uint4 v = __ldg(reinterpret_cast<const uint4*>(row + k0));
-            const uint32_t ids[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
-                                     v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
-            const uint32_t g = (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu;
+            float4* st = reinterpret_cast<float4*>(&stage[w][lane * 8]);
+            st[0] = make_float4(x[0], x[1], x[2], x[3]);
+            st[1] = make_float4(x[4], x[5], x[6], x[7]);
+        };
+        // Pass 1: totals over all positions in sorted order.
+        float tp = 0.0f, tn = 0.0f;
+        {
+            uint4 v = load(0);
+            for (int base = 0; base < n; base += 256) {
+                const uint4 vn = load(base + 256);
+                gather(base, v);
+                __syncwarp();
+                if (lane == 0) {
+                    const float4* st = reinterpret_cast<const float4*>(stage[w]);
+#pragma unroll 4
+                    for (int j = 0; j < 64; ++j) {
+                        const float4 q = st[j];
+                        const float e[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int k = k0 + i;
-                if (k < n - 1) {
-                    const float x = wsg[ids[i]];
-                    if (signbit(x))
-                        ln = __fadd_rn(ln, -x);
-                    else
-                        lp = __fadd_rn(lp, x);
-                    if ((g >> i) & 1u) {
-                        const float rp = __fsub_rn(tp, lp), rn = __fsub_rn(tn, ln);
-                        const float eL = __fadd_rn(ln, rp);
-                        if (eL < bestErr) {
-                            bestErr = eL;
-                            bestPar = -1;
-                            bestK = k;
-                        }
-                        const float eR = __fadd_rn(lp, rn);
-                        if (eR < bestErr || (eR == bestErr && bestPar < 1)) {
-                            bestErr = eR;
-                            bestPar = 1;
-                            bestK = k;
+                        for (int h = 0; h < 4; ++h) {
+                            const bool neg = signbit(e[h]);
+                            const float a = fabsf(e[h]);
+                            tp = __fadd_rn(tp, neg ? 0.0f : a);
+                            tn = __fadd_rn(tn, neg ? a : 0.0f);
                         }
                     }
                 }
+                __syncwarp();
+                v = vn;
             }
         }
-        if (bestK >= 0) {
-            refParity[f] = static_cast<int8_t>(bestPar);
-            refSplit[f] = bestK;
-            const unsigned long long key =
-                (static_cast<unsigned long long>(__float_as_uint(bestErr)) << 32) | static_cast<unsigned>(f);
-            atomicMin(&prm->winner, key);
+        tp = __shfl_sync(0xffffffffu, tp, 0);
+        tn = __shfl_sync(0xffffffffu, tn, 0);
+        // Pass 2: left sums after each position (lane 0), then every lane
+        // scores its 8 positions.  The reference's update rule over the
+        // candidates in split order (lower error replaces; at equal error
+        // parity +1 replaces parity -1) picks the lexicographic minimum of
+        // (error, parity +1 before -1, split index); errors are >= +0, so the
+        // float bits order like the values and the triple packs into one key.
+        unsigned long long best = ~0ull;
+        {
+            float lp = 0.0f, ln = 0.0f;
+            uint4 v = load(0);
+            for (int base = 0; base < n - 1; base += 256) {
+                const uint4 vn = load(base + 256);
+                gather(base, v);
+                __syncwarp();
+                if (lane == 0) {
+                    const float4* st = reinterpret_cast<const float4*>(stage[w]);
+#pragma unroll 4
+                    for (int j = 0; j < 64; ++j) {
+                        const float4 q = st[j];
+                        const float e[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                        for (int h = 0; h < 4; ++h) {
+                            const bool neg = signbit(e[h]);
+                            const float a = fabsf(e[h]);
+                            lp = __fadd_rn(lp, neg ? 0.0f : a);
+                            ln = __fadd_rn(ln, neg ? a : 0.0f);
+                            pre[w][4 * j + h] = make_float2(lp, ln);
+                        }
+                    }
+                }
+                __syncwarp();
+                const int k0 = base + lane * 8;
+                const uint32_t g = (k0 < n - 1) ? (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu : 0u;
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    if ((g >> h) & 1u) {
+                        const float2 l = pre[w][lane * 8 + h];
+                        const float eL = __fadd_rn(l.y, __fsub_rn(tp, l.x));  // parity -1
+                        const float eR = __fadd_rn(l.x, __fsub_rn(tn, l.y));  // parity +1
+                        const unsigned k = static_cast<unsigned>(k0 + h);
+                        const unsigned long long kL =
+                            (static_cast<unsigned long long>(__float_as_uint(eL)) << 32) | 0x80000000u | k;
+                        const unsigned long long kR = (static_cast<unsigned long long>(__float_as_uint(eR)) << 32) | k;
+                        best = min(best, min(kL, kR));
+                    }
+                }
+                __syncwarp();
+                v = vn;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+        if (lane == 0 && best != ~0ull) {
+            refParity[f] = (best & 0x80000000ull) ? int8_t(-1) : int8_t(1);
+            refSplit[f] = static_cast<int>(best & 0x7FFFFFFFull);
+            atomicMin(&prm->winner, (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f));
         }
     }
 }
@@ -1050,6 +1172,20 @@ int vj_trainer_bind(vj_trainer* t, const uint32_t* d_sumT, const float* d_invNor
     return ok();
 }
 
+int vj_trainer_last_round(vj_trainer* t, vj_round_info* out) {
+    if (!t || !out || !t->d_prm) return set_error(VJ_INVALID_ARG, "vj_trainer_last_round: no search has run");
+    RoundParams p;
+    VJ_CUDA_TRY(cudaDeviceSynchronize());
+    VJ_CUDA_TRY(cudaMemcpy(&p, t->d_prm, sizeof(p), cudaMemcpyDeviceToHost));
+    out->fastMin = bits_float(static_cast<int32_t>(p.fastMinBits));
+    out->window = p.window;
+    out->candidates = p.ncand;
+    out->status = p.status;
+    out->totalPos = p.tp;
+    out->totalNeg = p.tn;
+    return ok();
+}
+
 int vj_trainer_stage_bytes(vj_trainer* t, int n, int64_t* bytes) {
     if (!t || !bytes || n <= 0) return set_error(VJ_INVALID_ARG, "vj_trainer_stage_bytes: bad arguments");
     *bytes = t->nFeat * (((n + 7) & ~7) * 2 + ((n + 31) / 32) * 4);
@@ -1099,7 +1235,7 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         auto k = smemW ? refine_kernel<true> : refine_kernel<false>;
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("refine_kernel", s,
-                        k<<<sm_count(), 256, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg,
+                        k<<<2 * sm_count(), kRefineThreads, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg,
                                                           n, t->d_prm, t->d_cand, t->d_refParity, t->d_refSplit));
         VJ_LAUNCH_CHECK("refine_kernel");
     }

@@ -282,6 +282,21 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
  * the current stage.  Invalidated by vj_trainer_bind. */
 int vj_trainer_prepare_stage(vj_trainer* t, void* stream);
 
+/* Statistics of the last vj_stump_search (no reference counterpart): the
+ * fast-pass minimum error, the width of the candidate window, how many
+ * features were replayed exactly, and the active weight totals.  Copies from
+ * the device after synchronising the trainer's last stream. */
+typedef struct {
+    float fastMin;
+    float window;
+    int32_t candidates;
+    int32_t status;  /* 0 ok, 1 no valid split in any feature */
+    float totalPos;
+    float totalNeg;
+} vj_round_info;
+
+int vj_trainer_last_round(vj_trainer* t, vj_round_info* out);
+
 /* Resident memory used by vj_trainer_prepare_stage for n samples, in bytes. */
 int vj_trainer_stage_bytes(vj_trainer* t, int n, int64_t* bytes);
 
