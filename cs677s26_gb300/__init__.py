@@ -211,6 +211,42 @@ class FaceVisionEngine:
         res = [out[i * capPerImage: i * capPerImage + cnt[i]].copy() for i in range(n)]
         return Status(st), res
 
+    def lastStats(self) -> dict:
+        """Work counts and phase times of the last detectMultiScale / detectBatch call."""
+        rec = np.zeros(1, dtype=_capi.DETECT_STATS)
+        call("vj_detector_last_stats", self._h, ptr(rec))
+        out = {k: rec[k][0].item() for k in _capi.DETECT_STATS.names if k not in ("phaseMs", "hostMs")}
+        out["phaseMs"] = dict(zip(_capi.PHASES, [float(x) for x in rec["phaseMs"][0]]))
+        out["hostMs"] = dict(zip(_capi.HOST_PHASES, [float(x) for x in rec["hostMs"][0]]))
+        return out
+
+    def getConfig(self) -> dict:
+        rec = np.zeros(1, dtype=_capi.DETECT_CONFIG)
+        call("vj_detector_get_config", self._h, ptr(rec))
+        return {k: int(rec[k][0]) for k in _capi.DETECT_CONFIG.names}
+
+    def setConfig(self, **cfg) -> int:
+        """Launch shape of the detection kernel (tileRows, tileStumps, queueStumps, blocksPerSM)."""
+        cur = self.getConfig()
+        cur.update(cfg)
+        rec = np.zeros(1, dtype=_capi.DETECT_CONFIG)
+        for k, v in cur.items():
+            rec[k] = v
+        return Status(_capi.status("vj_detector_set_config", self._h, ptr(rec)))
+
+    def autotune(self, images, scaleFactor: float = 1.25, minObjectSize: int = 24, repeats: int = 2):
+        """Times the candidate launch shapes on `images`, keeps the fastest; returns (status, config, ms)."""
+        n = len(images)
+        on_dev = not isinstance(images[0], np.ndarray)
+        ptrs = (C.c_void_p * n)(*[ptr(im) for im in images])
+        ws = (C.c_int * n)(*[int(im.shape[1]) for im in images])
+        hs = (C.c_int * n)(*[int(im.shape[0]) for im in images])
+        rec = np.zeros(1, dtype=_capi.DETECT_CONFIG)
+        ms = C.c_double()
+        st = _capi.status("vj_detector_autotune", self._h, n, ptrs, ws, hs, ws, int(on_dev), C.c_float(scaleFactor),
+                          minObjectSize, repeats, ptr(rec), C.byref(ms))
+        return Status(st), {k: int(rec[k][0]) for k in _capi.DETECT_CONFIG.names}, ms.value
+
 
 class AdaBoostTrainer:
     """vj::AdaBoostTrainer: best-weak search and the AdaBoost round update."""

@@ -36,6 +36,15 @@ STAGE_CALIB = np.dtype([("cutVal", "<f4"), ("stageThreshold", "<f4"), ("strictGt
                         ("posPass", "<i4"), ("negSurvive", "<i4"), ("hitRate", "<f4"),
                         ("falseAlarm", "<f4"), ("satisfied", "<i4")])
 
+DETECT_STATS = np.dtype([("images", "<i8"), ("levels", "<i8"), ("pyramidPixels", "<i8"), ("windows", "<i8"),
+                         ("gated", "<i8"), ("stumpEvals", "<i8"), ("rawDetections", "<i8"), ("deepWindows", "<i8"),
+                         ("attempts", "<i4"), ("queuePasses", "<i4"), ("gpuMs", "<f8"), ("phaseMs", "<f8", 6),
+                         ("hostMs", "<f8", 3)])
+DETECT_CONFIG = np.dtype([("tileRows", "<i4"), ("tileStumps", "<i4"), ("queueStumps", "<i4"), ("blocksPerSM", "<i4")])
+PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "compaction")
+HOST_PHASES = ("plan_upload", "wait", "sort_group")
+
+assert DETECT_STATS.itemsize == 152 and DETECT_CONFIG.itemsize == 16
 assert HAAR_FEATURE.itemsize == 64 and STUMP4.itemsize == 16 and STAGE.itemsize == 12
 assert DETECTION.itemsize == 24 and TILE_BEST.itemsize == 16 and WEAK.itemsize == 28
 
@@ -84,6 +93,10 @@ SIGNATURES = {
     "vj_detect": (i32, [vp, vp, i32, i32, i32, i32, f32, i32, i32, i32, i32, vp, i32, pi32, vp]),
     "vj_group_rectangles": (i32, [vp, i32, i32, f32, vp, pi32]),
     "vj_detect_batch": (i32, [vp, i32, vp, vp, vp, vp, i32, f32, i32, i32, i32, i32, vp, i32, vp, vp]),
+    "vj_detector_last_stats": (i32, [vp, vp]),
+    "vj_detector_set_config": (i32, [vp, vp]),
+    "vj_detector_get_config": (i32, [vp, vp]),
+    "vj_detector_autotune": (i32, [vp, i32, vp, vp, vp, vp, i32, f32, i32, i32, vp, vp]),
     "vj_synth_patches": (i32, [u64, i32, i32, vp]),
     "vj_synth_scene": (i32, [u64, i32, i32, i32, i32, i32, vp]),
     "vj_synth_cascade": (i32, [u64, i32, i32, vp, vp]),

@@ -1,0 +1,677 @@
+// Device side of multiscale cascade detection: the records the detection
+// kernel reads, the window arithmetic, and the phases of the persistent
+// detection kernel.
+//
+// Window arithmetic follows the reference operation by operation
+// (src/face_vision_engine.cu:463-545 and its CPU twin src/main.cu:755-819):
+// float corners, (p0 - p1 - p2 + p3) * w per rectangle added in rectangle
+// order, raw * invNorm compared with theta, leaf values added in stump order
+// starting from 0.0f.  With --fmad=false and explicit __fadd_rn etc. the
+// results equal the reference CPU path bit for bit.
+#pragma once
+
+#include "integral_dev.cuh"
+
+namespace vjgb {
+
+// Stump record for per-lane global gathers (lane-per-window passes): corner
+// offsets of up to three rectangles relative to the window origin.
+struct alignas(16) DStump {
+    float theta, left, right;
+    int32_t nr;
+    float w[3];
+    int32_t pad0;
+    int8_t dx[12], dy[12];  // rectangle r, corner c at [4*r + c]
+    int32_t pad1[2];
+};
+static_assert(sizeof(DStump) == 64, "DStump is 64 bytes");
+
+// Stump record for the warp-per-window deep pass: corner offsets into the
+// window's (winW+1) x (winH+1) integral patch, which are the feature's own
+// p0..p3 indices (FastRect, common_types.cuh:26-35).  A 2-rectangle feature
+// has w2 == 0 and its third rectangle is not evaluated; for a 3-rectangle
+// feature with w2 == 0 skipping it is also exact, because adding the signed
+// zero v2 can only flip the sign of a zero raw, which compares equal.
+struct alignas(16) PStump {
+    float theta, left, right, w0;
+    float w1, w2;
+    uint32_t o[6];  // offsets 2k (low half) and 2k+1 (high half) of corners 0..11
+};
+static_assert(sizeof(PStump) == 48, "PStump is 48 bytes");
+
+struct DStage {
+    int32_t first, ntrees;
+    float threshold;
+    int32_t pad;
+};
+
+// One pyramid level of one image, as scanned.
+struct CasLevel {
+    const uint32_t* sum;
+    const uint64_t* sq;
+    int64_t pitch;
+    int workW, workH, step, scanW, scanH, tilesX;
+    int64_t tileBase;
+    float scale;
+    int scaleIdx;
+    int image;
+    int pad;
+};
+
+// Level k of an image is resized from level k-1 (or the image).
+struct ResizeJob {
+    const uint8_t* src;
+    int64_t srcStride;
+    int srcW, srcH;
+    uint8_t* dst;
+    int64_t dstStride;
+    int dstW, dstH;
+    float sx, sy;
+    int64_t itemBase;  // first work item (one warp per 128-pixel row chunk)
+};
+
+struct QEntry {
+    uint32_t level;
+    uint32_t xy;  // (y << 16) | x, window origin in level pixels
+    float inv;
+    float score;
+};
+
+constexpr int kCasThreads = 256;
+constexpr int kCasWarps = kCasThreads / 32;
+constexpr int kMaxQueuePasses = 6;
+constexpr int kQueues = kMaxQueuePasses + 2;
+constexpr int kPhaseStamps = 8;
+
+// Control block, zeroed before every launch and copied to the host after it.
+struct GridSync {
+    unsigned int arrive;
+    unsigned int error;  // set when a barrier wait ran out of time
+    unsigned int pad[2];
+    unsigned long long stamp[kPhaseStamps];  // %globaltimer at phase ends (block 0)
+};
+struct CtrlHead {
+    GridSync sync;
+    unsigned long long work[kQueues + 2];  // dynamic work counters of the passes
+    unsigned long long stats[4];           // [0] gated windows, [1] stump evaluations
+    int qcount[kQueues];                   // entries pushed to queue k (keeps counting past qcap)
+    int compactTotal;                      // raw detections copied to the host buffer
+    int compactOverflow;
+    // followed by int counts[imageCap] (raw detections per image, counting
+    // past detCap) and int offsets[imageCap] (start in the host buffer)
+};
+
+// Everything the persistent kernel reads: written by the host into pinned
+// memory and copied to the device by the first node of the launch graph.
+struct DevPlan {
+    int nImg, nLevels, nResize, nQueuePasses;
+    int winW, winH, normMode, nStages;
+    int tileStages, deepFrom, qcap, detCap;
+    int queueEnd[kMaxQueuePasses];  // stage range of queue pass m: [m ? queueEnd[m-1] : tileStages, queueEnd[m])
+    int hostCap, pad0;
+    int64_t totalTiles;
+    IIPlan ip;
+    const int* rjFirst;         // nResize + 1: resize jobs of chain position p
+    const int64_t* rjItems;     // nResize: work items of chain position p
+    const ResizeJob* rjobs;
+    const IIJob* iijobs;        // one per level
+    const CasLevel* levels;
+    uint32_t* totS;
+    uint64_t* totQ;
+    const DStump* stumps;
+    const PStump* pstumps;
+    const DStage* stages;
+    QEntry* q[2];
+    vj_detection* dets;         // nImg * detCap, image i at dets + i * detCap
+    CtrlHead* ctrl;
+    int* counts;                // in the control block
+    int* offsets;               // in the control block
+    vj_detection* hostDets;     // host-mapped, hostCap entries
+};
+
+// ---------------------------------------------------------------------------
+// Small device helpers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+constexpr unsigned long long kBarrierTimeoutNs = 60ull * 1000 * 1000 * 1000;  // 60 s
+constexpr unsigned kBarrierMaxSpins = 1u << 30;
+
+// Grid-wide barrier of the cooperative launch.  Every block arrives once per
+// barrier on a monotonic counter; the wait is bounded by time and by spin
+// count, after which the error flag is set.  Returns false (in every thread of
+// the block) once any block has set the error flag, so all blocks leave the
+// kernel instead of waiting again.
+__device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned& epoch) {
+    __shared__ int okShared;
+    __syncthreads();
+    ++epoch;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&g->arrive, 1u);
+        const unsigned target = epoch * gridDim.x;
+        const unsigned long long t0 = global_ns();
+        bool ok = true;
+        for (unsigned it = 0;; ++it) {
+            if (ld_acquire_u32(&g->arrive) >= target) break;
+            if (ld_acquire_u32(&g->error) != 0u) {
+                ok = false;
+                break;
+            }
+            if ((it & 127u) == 127u && (global_ns() - t0 > kBarrierTimeoutNs || it > kBarrierMaxSpins)) {
+                atomicExch(&g->error, 1u);
+                ok = false;
+                break;
+            }
+            __nanosleep(64);
+        }
+        if (ok && ld_acquire_u32(&g->error) != 0u) ok = false;
+        __threadfence();
+        okShared = ok ? 1 : 0;
+    }
+    __syncthreads();
+    __threadfence();
+    return okShared != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Pyramid resize (face_vision_engine.cu:270-308, main.cu:545-585): pixel-centre
+// bilinear with the reference's rounding, one warp per 128-pixel row chunk.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint8_t resize_px(const ResizeJob& J, int x, int y) {
+    const float fx = __fsub_rn(__fmul_rn(__fadd_rn(static_cast<float>(x), 0.5f), J.sx), 0.5f);
+    const float fy = __fsub_rn(__fmul_rn(__fadd_rn(static_cast<float>(y), 0.5f), J.sy), 0.5f);
+    const int sx0 = max(0, min(static_cast<int>(floorf(fx)), J.srcW - 1));
+    const int sy0 = max(0, min(static_cast<int>(floorf(fy)), J.srcH - 1));
+    const int sx1 = min(sx0 + 1, J.srcW - 1);
+    const int sy1 = min(sy0 + 1, J.srcH - 1);
+    const float ax = __fsub_rn(fx, static_cast<float>(sx0));
+    const float ay = __fsub_rn(fy, static_cast<float>(sy0));
+    const uint8_t* r0 = J.src + static_cast<size_t>(sy0) * J.srcStride;
+    const uint8_t* r1 = J.src + static_cast<size_t>(sy1) * J.srcStride;
+    const float p00 = static_cast<float>(r0[sx0]), p01 = static_cast<float>(r0[sx1]);
+    const float p10 = static_cast<float>(r1[sx0]), p11 = static_cast<float>(r1[sx1]);
+    const float top = __fadd_rn(p00, __fmul_rn(__fsub_rn(p01, p00), ax));
+    const float bot = __fadd_rn(p10, __fmul_rn(__fsub_rn(p11, p10), ax));
+    const float val = __fadd_rn(top, __fmul_rn(__fsub_rn(bot, top), ay));
+    const int v = __float2int_rz(__fadd_rn(val, 0.5f));
+    return static_cast<uint8_t>(v < 0 ? 0 : (v > 255 ? 255 : v));
+}
+
+__device__ __forceinline__ void resize_item(const ResizeJob* __restrict__ jobs, int njobs, int64_t it, int lane) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].itemBase <= it) lo = mid; else hi = mid - 1;
+    }
+    const ResizeJob J = jobs[lo];
+    const int chunks = (J.dstW + 127) >> 7;
+    const int64_t local = it - J.itemBase;
+    const int y = static_cast<int>(local / chunks);
+    const int x0 = static_cast<int>(local % chunks) * 128 + lane * 4;
+    uint8_t* drow = J.dst + static_cast<size_t>(y) * J.dstStride;
+    if (x0 + 4 <= J.dstW) {
+        uchar4 v;
+        v.x = resize_px(J, x0, y);
+        v.y = resize_px(J, x0 + 1, y);
+        v.z = resize_px(J, x0 + 2, y);
+        v.w = resize_px(J, x0 + 3, y);
+        *reinterpret_cast<uchar4*>(drow + x0) = v;
+    } else {
+        for (int i = 0; i < 4; ++i)
+            if (x0 + i < J.dstW) drow[x0 + i] = resize_px(J, x0 + i, y);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Window evaluation.
+// ---------------------------------------------------------------------------
+
+// Variance gate (face_vision_engine.cu:463-492); returns invNorm, or 0 when
+// the window is rejected.
+__device__ __forceinline__ float window_inv(const CasLevel& L, int x, int y, int winW, int winH, int normMode) {
+    const int64_t P = L.pitch;
+    const int nw = winW - 2, nh = winH - 2;
+    const int64_t b = static_cast<int64_t>(y) * P + x;
+    const int64_t o0 = b + P + 1, o1 = b + P + 1 + nw, o2 = b + (1 + nh) * P + 1, o3 = b + (1 + nh) * P + 1 + nw;
+    const uint32_t s0 = L.sum[o0], s1 = L.sum[o1], s2 = L.sum[o2], s3 = L.sum[o3];
+    double ns;
+    if (normMode == VJ_NORM_FLOAT_CORNERS) {
+        ns = static_cast<double>(
+            __fadd_rn(__fsub_rn(__fsub_rn(corner_f(s0), corner_f(s1)), corner_f(s2)), corner_f(s3)));
+    } else {
+        ns = static_cast<double>(static_cast<int32_t>(s0 - s1 - s2 + s3));
+    }
+    const uint32_t q = static_cast<uint32_t>(L.sq[o0]) - static_cast<uint32_t>(L.sq[o1]) -
+                       static_cast<uint32_t>(L.sq[o2]) + static_cast<uint32_t>(L.sq[o3]);
+    const double area = static_cast<double>(nw * nh);
+    const double nf2 = __dsub_rn(__dmul_rn(area, static_cast<double>(q)), __dmul_rn(ns, ns));
+    if (!(nf2 > 0.0)) return 0.0f;
+    const float inv = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(nf2)));
+    if (!(__dmul_rn(area, static_cast<double>(inv)) < 1e-1)) return 0.0f;
+    return inv;
+}
+
+// Leaf value of one stump for the window at level offset `b`, corners
+// gathered from the level's integral image (main.cu:785-797).
+__device__ __forceinline__ float stump_value(const DStump* __restrict__ sp, const uint32_t* sum, int64_t P, int64_t b,
+                                             float inv) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(sp));
+    const float4 wv = __ldg(reinterpret_cast<const float4*>(sp) + 1);
+    const int4 d = __ldg(reinterpret_cast<const int4*>(sp) + 2);
+    const int4 e = __ldg(reinterpret_cast<const int4*>(sp) + 3);
+    const int nr = __float_as_int(a.w);
+    const uint32_t dxw[3] = {static_cast<uint32_t>(d.x), static_cast<uint32_t>(d.y), static_cast<uint32_t>(d.z)};
+    const uint32_t dyw[3] = {static_cast<uint32_t>(d.w), static_cast<uint32_t>(e.x), static_cast<uint32_t>(e.y)};
+    const float wr[3] = {wv.x, wv.y, wv.z};
+    float raw = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        if (r < nr) {
+            float c[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int ci = 4 * r + q;
+                const int dx = static_cast<int8_t>((dxw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
+                const int dy = static_cast<int8_t>((dyw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
+                c[q] = corner_f(sum[b + dy * P + dx]);
+            }
+            const float v = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(c[0], c[1]), c[2]), c[3]), wr[r]);
+            raw = (r == 0) ? v : __fadd_rn(raw, v);
+        }
+    }
+    return __fmul_rn(raw, inv) < a.x ? a.y : a.z;
+}
+
+// Sum of one stage's stumps for one window, added in stump order.  Four
+// stumps are evaluated before their values are added so their integral loads
+// are in flight together; the additions keep the reference's order.
+__device__ __forceinline__ float stage_sum(const DStump* __restrict__ stumps, const DStage& st, const uint32_t* sum,
+                                           int64_t P, int64_t b, float inv) {
+    const DStump* sp = stumps + st.first;
+    float acc = 0.0f;
+    int k = 0;
+    for (; k + 4 <= st.ntrees; k += 4) {
+        const float c0 = stump_value(sp + k, sum, P, b, inv);
+        const float c1 = stump_value(sp + k + 1, sum, P, b, inv);
+        const float c2 = stump_value(sp + k + 2, sum, P, b, inv);
+        const float c3 = stump_value(sp + k + 3, sum, P, b, inv);
+        acc = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(acc, c0), c1), c2), c3);
+    }
+    for (; k < st.ntrees; ++k) acc = __fadd_rn(acc, stump_value(sp + k, sum, P, b, inv));
+    return acc;
+}
+
+// Leaf value of one stump from the window's integral patch in shared memory
+// (corners already converted to float).
+__device__ __forceinline__ float patch_stump_value(const PStump* __restrict__ sp, const float* patch, float inv) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(sp));
+    const uint4 b = __ldg(reinterpret_cast<const uint4*>(sp) + 1);
+    const uint4 c = __ldg(reinterpret_cast<const uint4*>(sp) + 2);
+    const float w1 = __uint_as_float(b.x), w2 = __uint_as_float(b.y);
+    const float v0 = __fmul_rn(
+        __fadd_rn(__fsub_rn(__fsub_rn(patch[b.z & 0xFFFFu], patch[b.z >> 16]), patch[b.w & 0xFFFFu]), patch[b.w >> 16]),
+        a.w);
+    const float v1 = __fmul_rn(
+        __fadd_rn(__fsub_rn(__fsub_rn(patch[c.x & 0xFFFFu], patch[c.x >> 16]), patch[c.y & 0xFFFFu]), patch[c.y >> 16]),
+        w1);
+    float raw = __fadd_rn(v0, v1);
+    if (w2 != 0.0f) {
+        const float v2 = __fmul_rn(
+            __fadd_rn(__fsub_rn(__fsub_rn(patch[c.z & 0xFFFFu], patch[c.z >> 16]), patch[c.w & 0xFFFFu]),
+                      patch[c.w >> 16]),
+            w2);
+        raw = __fadd_rn(raw, v2);
+    }
+    return __fmul_rn(raw, inv) < a.x ? a.y : a.z;
+}
+
+// Output record of a window (face_vision_engine.cu:559-567): level
+// coordinates scaled by the level's scale and rounded as the reference does.
+__device__ __forceinline__ vj_detection make_detection(const CasLevel& L, const QEntry& e, int winW, int winH,
+                                                       float score) {
+    const int x = static_cast<int>(e.xy & 0xFFFFu), y = static_cast<int>(e.xy >> 16);
+    vj_detection d;
+    d.x = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(x), L.scale), 0.5f));
+    d.y = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(y), L.scale), 0.5f));
+    d.w = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(winW), L.scale), 0.5f));
+    d.h = __float2int_rz(__fadd_rn(__fmul_rn(static_cast<float>(winH), L.scale), 0.5f));
+    d.scaleIdx = L.scaleIdx;
+    d.score = score;
+    return d;
+}
+
+// Warp-wide emission of the valid lanes' windows: one atomic per image
+// present in the warp; the per-image counters keep counting past detCap so
+// the host sees an overflow.
+__device__ __forceinline__ void emit_warp(const DevPlan& P, const QEntry& e, bool valid) {
+    const unsigned m = __ballot_sync(0xffffffffu, valid);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int image = valid ? P.levels[e.level].image : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, image);
+    int base = 0;
+    const int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) base = atomicAdd(P.counts + image, __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!valid) return;
+    const int slot = base + __popc(peers & lanemask_lt());
+    if (slot < P.detCap)
+        P.dets[static_cast<size_t>(image) * P.detCap + slot] = make_detection(P.levels[e.level], e, P.winW, P.winH, e.score);
+}
+
+// Appends the valid lanes' entries to a queue with one atomic per warp.
+__device__ __forceinline__ void push_queue(QEntry* __restrict__ q, int* __restrict__ qcount, int qcap, bool valid,
+                                           const QEntry& e) {
+    const unsigned m = __ballot_sync(0xffffffffu, valid);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(qcount, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (valid) {
+        const int slot = base + __popc(m & lanemask_lt());
+        if (slot < qcap) q[slot] = e;
+    }
+}
+
+__device__ __forceinline__ int find_level(const CasLevel* __restrict__ levels, int n, int64_t t) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (levels[mid].tileBase <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Lane-per-window pass.  Each warp repeatedly takes a batch of windows - a
+// 32 x TH tile of window positions of some level (after the variance gate) in
+// the tile pass, or a chunk of queue entries in a queue pass - into a private
+// list in shared memory, runs stages [s0, s1) over it 32 windows at a time,
+// and after every stage compacts the survivors with a ballot, so the next
+// stage again runs on full warps.  Survivors go to the next queue, or become
+// detections when s1 is the last stage.
+// ---------------------------------------------------------------------------
+template <int TH>
+__device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const QEntry* qin, int qinCount, int s0,
+                                          int s1, unsigned long long* workCounter, QEntry* qout, int* qoutCount,
+                                          unsigned long long& gated, unsigned long long& evals) {
+    constexpr int kCap = 32 * TH;
+    const int lane = threadIdx.x & 31;
+    const bool last = s1 >= P.nStages;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(workCounter, 1ull);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        int count = 0;
+        if (qin == nullptr) {
+            if (t >= static_cast<unsigned long long>(P.totalTiles)) break;
+            const int li = find_level(P.levels, P.nLevels, static_cast<int64_t>(t));
+            const CasLevel L = P.levels[li];
+            const int64_t local = static_cast<int64_t>(t) - L.tileBase;
+            const int tx = static_cast<int>(local % L.tilesX), ty = static_cast<int>(local / L.tilesX);
+            for (int r = 0; r < TH; ++r) {
+                const int gx = tx * 32 + lane, gy = ty * TH + r;
+                const int x = gx * L.step, y = gy * L.step;
+                float iv = 0.0f;
+                if (gx < L.scanW && gy < L.scanH) iv = window_inv(L, x, y, P.winW, P.winH, P.normMode);
+                const bool ok = iv != 0.0f;
+                const unsigned m = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    QEntry e;
+                    e.level = static_cast<uint32_t>(li);
+                    e.xy = (static_cast<uint32_t>(y) << 16) | static_cast<uint32_t>(x);
+                    e.inv = iv;
+                    e.score = 0.0f;
+                    lst[count + __popc(m & lanemask_lt())] = e;
+                }
+                count += __popc(m);
+            }
+            gated += static_cast<unsigned>(count);
+        } else {
+            // Entries per take: enough to keep every warp busy, 32 to kCap.
+            const int n = qinCount;
+            const int warps = gridDim.x * kCasWarps;
+            const int chunk = min(kCap, max(32, ((n + warps - 1) / warps + 31) & ~31));
+            const int64_t base = static_cast<int64_t>(t) * chunk;
+            if (base >= n) break;
+            count = static_cast<int>(n - base < chunk ? n - base : chunk);
+            for (int i = lane; i < count; i += 32) lst[i] = qin[base + i];
+        }
+        __syncwarp();
+        for (int si = s0; si < s1 && count > 0; ++si) {
+            const DStage st = P.stages[si];
+            evals += static_cast<unsigned long long>(count) * static_cast<unsigned>(st.ntrees);
+            int nc = 0;
+            for (int g = 0; g < count; g += 32) {
+                const int i = g + lane;
+                const bool act = i < count;
+                QEntry e{};
+                float s = 0.0f;
+                if (act) {
+                    e = lst[i];
+                    const CasLevel& L = P.levels[e.level];
+                    const int64_t Pi = L.pitch;
+                    const int64_t b = static_cast<int64_t>(e.xy >> 16) * Pi + static_cast<int64_t>(e.xy & 0xFFFFu);
+                    s = stage_sum(P.stumps, st, L.sum, Pi, b, e.inv);
+                }
+                const bool pass = act && !(s < st.threshold);
+                const unsigned m = __ballot_sync(0xffffffffu, pass);
+                __syncwarp();
+                if (pass) {
+                    e.score = s;
+                    lst[nc + __popc(m & lanemask_lt())] = e;
+                }
+                nc += __popc(m);
+                __syncwarp();
+            }
+            count = nc;
+        }
+        for (int g = 0; g < count; g += 32) {
+            const int i = g + lane;
+            const bool act = i < count;
+            QEntry e{};
+            if (act) e = lst[i];
+            if (last)
+                emit_warp(P, e, act);
+            else
+                push_queue(qout, qoutCount, P.qcap, act, e);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-per-window deep pass.  A warp takes one window at a time, copies its
+// (winW+1) x (winH+1) integral patch into shared memory as floats, and runs
+// the remaining stages with lane k evaluating stump k of each group of 32; the
+// stage sum then adds the 32 leaf values in stump order (shuffles from lane
+// 0, 1, ...), so it is the same sequential fp32 sum as the reference's.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void deep_pass(const DevPlan& P, float* patch, const QEntry* q, int n,
+                                          unsigned long long* workCounter, unsigned long long& evals) {
+    const int lane = threadIdx.x & 31;
+    const int pw = P.winW + 1, ph = P.winH + 1;
+    const int warps = gridDim.x * kCasWarps;
+    const int take = max(1, min(16, n / (warps * 8)));
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(workCounter, static_cast<unsigned long long>(take));
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= static_cast<unsigned long long>(n)) break;
+        const int end = static_cast<int>(min(static_cast<unsigned long long>(n), t + take));
+        for (int i = static_cast<int>(t); i < end; ++i) {
+            const QEntry e = q[i];
+            const CasLevel& L = P.levels[e.level];
+            const uint32_t* sum = L.sum;
+            const int64_t Pi = L.pitch;
+            const int64_t b = static_cast<int64_t>(e.xy >> 16) * Pi + static_cast<int64_t>(e.xy & 0xFFFFu);
+            __syncwarp();
+            for (int r = 0; r < ph; ++r)
+                for (int c = lane; c < pw; c += 32) patch[r * pw + c] = corner_f(sum[b + r * Pi + c]);
+            __syncwarp();
+            float score = e.score;
+            bool alive = true;
+            for (int si = P.deepFrom; si < P.nStages; ++si) {
+                const DStage st = P.stages[si];
+                const PStump* sp = P.pstumps + st.first;
+                float acc = 0.0f;
+                for (int k0 = 0; k0 < st.ntrees; k0 += 32) {
+                    const int k = k0 + lane;
+                    float c = 0.0f;
+                    if (k < st.ntrees) c = patch_stump_value(sp + k, patch, e.inv);
+                    const int m = min(32, st.ntrees - k0);
+                    if (m == 32) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, c, j));
+                    } else {
+                        for (int j = 0; j < m; ++j) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, c, j));
+                    }
+                }
+                evals += static_cast<unsigned>(st.ntrees);
+                if (acc < st.threshold) {
+                    alive = false;
+                    break;
+                }
+                score = acc;
+            }
+            if (alive && lane == 0) {
+                const int image = L.image;
+                const int slot = atomicAdd(P.counts + image, 1);
+                if (slot < P.detCap)
+                    P.dets[static_cast<size_t>(image) * P.detCap + slot] = make_detection(L, e, P.winW, P.winH, score);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The persistent detection kernel: every phase of a batch in one cooperative
+// launch, phases separated by grid barriers.
+//   1. pyramid: resize chain positions 0, 1, ... (level k from level k-1);
+//   2. integral images of every level: row pass, column totals, column scan;
+//   3. tile pass (lane-per-window) over every level of every image;
+//   4. lane-per-window queue passes (optional);
+//   5. warp-per-window deep pass over the remaining stages;
+//   6. compaction of the raw detections, image after image, into the
+//      host-mapped buffer.
+// ---------------------------------------------------------------------------
+template <int TH>
+__global__ void __launch_bounds__(kCasThreads)
+detect_persistent_kernel(const DevPlan* __restrict__ plan) {
+    extern __shared__ __align__(16) unsigned char dsmem[];
+    const DevPlan& P = *plan;
+    CtrlHead* C = P.ctrl;
+    GridSync* G = &C->sync;
+    unsigned epoch = 0;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const bool stamper = blockIdx.x == 0 && threadIdx.x == 0;
+    if (stamper) G->stamp[0] = global_ns();
+
+    // 1. pyramid
+    for (int p = 0; p < P.nResize; ++p) {
+        const int j0 = P.rjFirst[p], j1 = P.rjFirst[p + 1];
+        const int64_t items = P.rjItems[p];
+        for (int64_t it = gw; it < items; it += nw) resize_item(P.rjobs + j0, j1 - j0, it, lane);
+        if (!grid_barrier(G, epoch)) return;
+    }
+    if (stamper) G->stamp[1] = global_ns();
+
+    // 2. integral images
+    for (int64_t r = gw; r < P.ip.rows; r += nw) ii_row_item(P.iijobs, P.nLevels, r, lane);
+    if (!grid_barrier(G, epoch)) return;
+    for (int64_t it = gw; it < P.ip.items; it += nw)
+        ii_col_total_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
+    if (!grid_barrier(G, epoch)) return;
+    for (int64_t it = gw; it < P.ip.items; it += nw)
+        ii_col_scan_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
+    if (!grid_barrier(G, epoch)) return;
+    if (stamper) G->stamp[2] = global_ns();
+
+    unsigned long long gated = 0, evals = 0;
+    QEntry* lst = reinterpret_cast<QEntry*>(dsmem) + static_cast<size_t>(wib) * 32 * TH;
+
+    // 3. tile pass -> queue 0 (or detections)
+    lane_pass<TH>(P, lst, nullptr, 0, 0, P.tileStages, &C->work[0], P.q[0], &C->qcount[0], gated, evals);
+    if (!grid_barrier(G, epoch)) return;
+    if (stamper) G->stamp[3] = global_ns();
+
+    // 4. queue passes: queue m -> queue m+1
+    for (int m = 0; m < P.nQueuePasses; ++m) {
+        const int s0 = m == 0 ? P.tileStages : P.queueEnd[m - 1];
+        const int nIn = min(C->qcount[m], P.qcap);
+        lane_pass<TH>(P, lst, P.q[m & 1], nIn, s0, P.queueEnd[m], &C->work[1 + m], P.q[(m + 1) & 1],
+                      &C->qcount[m + 1], gated, evals);
+        if (!grid_barrier(G, epoch)) return;
+    }
+    if (stamper) G->stamp[4] = global_ns();
+
+    // 5. deep pass
+    if (P.deepFrom < P.nStages) {
+        const int m = P.nQueuePasses;
+        const int nIn = min(C->qcount[m], P.qcap);
+        float* patch = reinterpret_cast<float*>(dsmem) + static_cast<size_t>(wib) * (P.winW + 1) * (P.winH + 1);
+        deep_pass(P, patch, P.q[m & 1], nIn, &C->work[kQueues], evals);
+    }
+    if (lane == 0) {
+        if (gated) atomicAdd(&C->stats[0], gated);
+        if (evals) atomicAdd(&C->stats[1], evals);
+    }
+    if (!grid_barrier(G, epoch)) return;
+    if (stamper) G->stamp[5] = global_ns();
+
+    // 6. compaction: block 0 lays out the images' raw detections in the host
+    // buffer, then every warp copies 32-record chunks.
+    if (blockIdx.x == 0) {
+        __shared__ int part[kCasThreads];
+        const int n = P.nImg;
+        const int per = (n + kCasThreads - 1) / kCasThreads;
+        const int i0 = threadIdx.x * per, i1 = min(n, i0 + per);
+        int s = 0;
+        for (int i = i0; i < i1; ++i) s += min(P.counts[i], P.detCap);
+        part[threadIdx.x] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int k = 0; k < kCasThreads; ++k) {
+                const int v = part[k];
+                part[k] = run;
+                run += v;
+            }
+            C->compactTotal = run;
+            C->compactOverflow = run > P.hostCap ? 1 : 0;
+        }
+        __syncthreads();
+        int off = part[threadIdx.x];
+        for (int i = i0; i < i1; ++i) {
+            P.offsets[i] = off;
+            off += min(P.counts[i], P.detCap);
+        }
+    }
+    if (!grid_barrier(G, epoch)) return;
+    if (C->compactOverflow == 0) {
+        for (int64_t i = gw; i < P.nImg; i += nw) {
+            const int cnt = min(P.counts[i], P.detCap);
+            const int off = P.offsets[i];
+            const vj_detection* src = P.dets + static_cast<size_t>(i) * P.detCap;
+            for (int k = lane; k < cnt; k += 32) P.hostDets[off + k] = src[k];
+        }
+    }
+    if (stamper) G->stamp[6] = global_ns();
+}
+
+}  // namespace vjgb

@@ -22,7 +22,7 @@
 #include <string>
 #include <vector>
 
-#include "integral.cuh"
+#include "integral_dev.cuh"
 
 namespace vjgb {
 namespace {
@@ -141,152 +141,33 @@ train_integral_generic_kernel(const uint8_t* __restrict__ gray, int w, int h, in
     }
 }
 
-__device__ __forceinline__ int find_job(const IIJob* __restrict__ jobs, int njobs, int64_t item, bool byRow) {
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        const int64_t b = byRow ? jobs[mid].rowBase : jobs[mid].itemBase;
-        if (b <= item)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    return lo;
-}
-
-// Row pass: integral row 0 is zero; row y >= 1 holds, at column c, the sum of
-// pixels [0, c) of image row y-1 (and the sum of their squares).
+// Row pass: one warp per integral row (integral_dev.cuh).
 __global__ void __launch_bounds__(256)
 row_pass_kernel(const IIJob* __restrict__ jobs, int njobs, int64_t rows) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    for (int64_t r = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < rows; r += nw) {
-        const IIJob J = jobs[find_job(jobs, njobs, r, true)];
-        const int y = static_cast<int>(r - J.rowBase);
-        uint32_t* srow = J.sum + static_cast<size_t>(y) * J.pitch;
-        uint64_t* qrow = J.sq + static_cast<size_t>(y) * J.pitch;
-        const bool vecOut = ((J.pitch & 3) == 0) && ((reinterpret_cast<uintptr_t>(J.sum) & 15) == 0) &&
-                            ((reinterpret_cast<uintptr_t>(J.sq) & 15) == 0);
-        const uint8_t* prow = y > 0 ? J.pix + static_cast<size_t>(y - 1) * J.stride : nullptr;
-        uint32_t carryS = 0, carryQ = 0;
-        for (int cb = 0; cb <= J.w; cb += 512) {
-            const int c0 = cb + lane * 16;
-            uint32_t p[16];
-            if (y == 0) {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) p[i] = 0;
-            } else if (c0 + 16 <= J.w && ((reinterpret_cast<uintptr_t>(prow + c0) & 15) == 0)) {
-                const uint4 v = __ldg(reinterpret_cast<const uint4*>(prow + c0));
-                const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                for (int i = 0; i < 16; ++i) p[i] = (wv[i >> 2] >> (8 * (i & 3))) & 0xFFu;
-            } else {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) p[i] = (c0 + i < J.w) ? __ldg(prow + c0 + i) : 0u;
-            }
-            uint32_t es[16], eq[16];
-            uint32_t ls = 0, lq = 0;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                es[i] = ls;
-                eq[i] = lq;
-                ls += p[i];
-                lq += p[i] * p[i];
-            }
-            uint32_t is = ls, iq = lq;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t ys = __shfl_up_sync(0xffffffffu, is, o);
-                const uint32_t yq = __shfl_up_sync(0xffffffffu, iq, o);
-                if (lane >= o) {
-                    is += ys;
-                    iq += yq;
-                }
-            }
-            const uint32_t bs = carryS + is - ls, bq = carryQ + iq - lq;
-            carryS += __shfl_sync(0xffffffffu, is, 31);
-            carryQ += __shfl_sync(0xffffffffu, iq, 31);
-            if (vecOut && c0 + 15 <= J.w) {
-                uint4* so = reinterpret_cast<uint4*>(srow + c0);
-                ulonglong2* qo = reinterpret_cast<ulonglong2*>(qrow + c0);
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    so[i] = make_uint4(bs + es[4 * i], bs + es[4 * i + 1], bs + es[4 * i + 2], bs + es[4 * i + 3]);
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    qo[i] = make_ulonglong2(static_cast<uint64_t>(bq + eq[2 * i]),
-                                            static_cast<uint64_t>(bq + eq[2 * i + 1]));
-            } else {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    if (c0 + i <= J.w) {
-                        srow[c0 + i] = bs + es[i];
-                        qrow[c0 + i] = static_cast<uint64_t>(bq + eq[i]);
-                    }
-                }
-            }
-        }
-    }
+    for (int64_t r = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < rows; r += nw)
+        ii_row_item(jobs, njobs, r, lane);
 }
 
-__device__ __forceinline__ void col_item(const IIJob& J, int64_t local, int lane, int* seg, int* c, int* r0, int* r1) {
-    const int chunks = (J.w + 1 + 31) >> 5;
-    *seg = static_cast<int>(local / chunks);
-    *c = static_cast<int>(local % chunks) * 32 + lane;
-    *r0 = 1 + *seg * kColSeg;
-    *r1 = min(J.h, (*seg + 1) * kColSeg);
-}
-
-// Column pass A: per 32-row segment and column, the sum of the row prefixes.
+// Column pass A: segment totals.
 __global__ void __launch_bounds__(256)
 col_total_kernel(const IIJob* __restrict__ jobs, int njobs, int64_t items, int64_t totPitch,
                  uint32_t* __restrict__ totS, uint64_t* __restrict__ totQ) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    for (int64_t it = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; it < items; it += nw) {
-        const IIJob J = jobs[find_job(jobs, njobs, it, false)];
-        int seg, c, r0, r1;
-        col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
-        if (c > J.w) continue;
-        uint32_t s = 0;
-        uint64_t q = 0;
-        for (int r = r0; r <= r1; ++r) {
-            s += __ldg(J.sum + static_cast<size_t>(r) * J.pitch + c);
-            q += __ldg(J.sq + static_cast<size_t>(r) * J.pitch + c);
-        }
-        const size_t o = static_cast<size_t>(J.totBase + seg) * totPitch + c;
-        totS[o] = s;
-        totQ[o] = q;
-    }
+    for (int64_t it = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; it < items; it += nw)
+        ii_col_total_item(jobs, njobs, it, lane, totPitch, totS, totQ);
 }
 
-// Column pass B: carry of the segments above, then the running column sum
-// written in place.
+// Column pass B: in-place column scan.
 __global__ void __launch_bounds__(256)
 col_scan_kernel(const IIJob* __restrict__ jobs, int njobs, int64_t items, int64_t totPitch,
                 const uint32_t* __restrict__ totS, const uint64_t* __restrict__ totQ) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    for (int64_t it = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; it < items; it += nw) {
-        const IIJob J = jobs[find_job(jobs, njobs, it, false)];
-        int seg, c, r0, r1;
-        col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
-        if (c > J.w) continue;
-        uint32_t s = 0;
-        uint64_t q = 0;
-        for (int k = 0; k < seg; ++k) {
-            const size_t o = static_cast<size_t>(J.totBase + k) * totPitch + c;
-            s += totS[o];
-            q += totQ[o];
-        }
-        for (int r = r0; r <= r1; ++r) {
-            const size_t o = static_cast<size_t>(r) * J.pitch + c;
-            s += J.sum[o];
-            q += J.sq[o];
-            J.sum[o] = s;
-            J.sq[o] = q;
-        }
-    }
+    for (int64_t it = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; it < items; it += nw)
+        ii_col_scan_item(jobs, njobs, it, lane, totPitch, totS, totQ);
 }
 
 int grid_for(int64_t warps) {

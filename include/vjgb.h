@@ -387,6 +387,55 @@ int vj_detect_batch(vj_detector* d, int n, const uint8_t* const* images,
                     int minObjectSize, int maxDetectionsPerImage, int applyGrouping,
                     vj_detection* out, int capPerImage, int* counts, void* stream);
 
+/* Work counts and phase times of the last vj_detect / vj_detect_batch call on
+ * a detector (no reference counterpart; the windows/s and stumps/s figures of
+ * a run). */
+typedef struct vj_detect_stats {
+    int64_t images;          /* images in the call */
+    int64_t levels;          /* pyramid levels scanned */
+    int64_t pyramidPixels;   /* pixels of every scanned level */
+    int64_t windows;         /* window positions on the levels' scan grids */
+    int64_t gated;           /* windows through the variance gate */
+    int64_t stumpEvals;      /* stump evaluations */
+    int64_t rawDetections;   /* windows through every stage, before truncation */
+    int64_t deepWindows;     /* windows entering the warp-per-window deep pass */
+    int32_t attempts;        /* 1, or more when a work buffer had to grow */
+    int32_t queuePasses;     /* lane-per-window queue passes after the tile pass */
+    double gpuMs;            /* device time of the detection launch */
+    double phaseMs[6];       /* pyramid, integrals, tile pass, queue passes,
+                                deep pass, compaction of the raw detections */
+    double hostMs[3];        /* host wall time: planning and upload, waiting
+                                for the device, sorting and grouping */
+} vj_detect_stats;
+
+int vj_detector_last_stats(const vj_detector* d, vj_detect_stats* out);
+
+/* Launch shape of the detection kernel (no reference counterpart).  Every
+ * configuration gives the same detections; they differ only in speed. */
+typedef struct vj_detect_config {
+    int32_t tileRows;     /* rows of the 32-wide window tile a warp scans in
+                             the tile pass: 4, 8 or 16 */
+    int32_t tileStumps;   /* the tile pass runs whole stages until it has
+                             covered at least this many stumps */
+    int32_t queueStumps;  /* lane-per-window queue passes then cover at least
+                             this many more stumps (0 = none) before the
+                             warp-per-window deep pass takes the rest */
+    int32_t blocksPerSM;  /* persistent CTAs per SM; 0 = as many as fit */
+} vj_detect_config;
+
+int vj_detector_set_config(vj_detector* d, const vj_detect_config* cfg);
+int vj_detector_get_config(const vj_detector* d, vj_detect_config* cfg);
+
+/* Autotuner: runs every candidate configuration on the given images
+ * (vj_detect_batch arguments, without grouping), `repeats` timed launches
+ * each, checks that each candidate's raw detections equal the first
+ * candidate's, and keeps the fastest on the detector.  *chosen and *chosenMs
+ * (median device ms of the winner) may be null. */
+int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images,
+                         const int* w, const int* h, const int* stride,
+                         int images_on_device, float scaleFactor, int minObjectSize,
+                         int repeats, vj_detect_config* chosen, double* chosenMs);
+
 /* ------------------------------------------------------------------------ */
 /* Synthetic inputs (no reference counterpart: they stand in for the Kaggle  */
 /* faces, COCO negatives and demo images the reference trains and detects   */

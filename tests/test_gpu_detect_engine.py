@@ -1,0 +1,114 @@
+"""Detection engine: launch shapes, the autotuner and the work counters.
+
+Every launch shape (tile rows, tile-pass depth, lane-per-window queue passes,
+CTAs per SM) must give the raw detections of the oracle's restatement of
+detectMultiScaleCpu (src/main.cu:684-827) bit for bit; the autotuner checks
+the same across its candidates and keeps one of them.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CONFIGS = [
+    dict(tileRows=8, tileStumps=64, queueStumps=0, blocksPerSM=0),
+    dict(tileRows=4, tileStumps=1, queueStumps=0, blocksPerSM=0),
+    dict(tileRows=16, tileStumps=111, queueStumps=0, blocksPerSM=0),
+    dict(tileRows=8, tileStumps=36, queueStumps=400, blocksPerSM=0),
+    dict(tileRows=8, tileStumps=11, queueStumps=2000, blocksPerSM=2),
+    dict(tileRows=4, tileStumps=100000, queueStumps=0, blocksPerSM=1),
+]
+
+
+@pytest.fixture(scope="module")
+def full_case(vj, oracle, basic_pool):
+    st, sg = vj.synth_cascade(2)
+    scene = vj.synth_scene(7, 800, 600, 12, 24, 200)
+    ref = oracle.detect(basic_pool, st, sg, scene, norm_mode=0, threads=8)
+    return st, sg, scene, ref
+
+
+def engine(vj, pool, st, sg, maxdet=200000):
+    e = vj.FaceVisionEngine((24, 24), 1, 3840, 2160, False, maxdet)
+    assert e.setCascadeModel(pool.view(vj.HAAR_FEATURE), st.view(vj.STUMP4), sg.view(vj.STAGE)) == 0
+    return e
+
+
+@pytest.mark.parametrize("cfg", CONFIGS, ids=[f"th{c['tileRows']}-t{c['tileStumps']}-q{c['queueStumps']}-b"
+                                              f"{c['blocksPerSM']}" for c in CONFIGS])
+def test_every_launch_shape_matches_oracle(cuda, vj, basic_pool, full_case, cfg):
+    st, sg, scene, ref = full_case
+    e = engine(vj, basic_pool, st, sg)
+    assert e.setConfig(**cfg) == 0
+    assert e.getConfig() == cfg
+    h, w = scene.shape
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0
+    assert len(raw) == len(ref) and raw.tobytes() == ref.tobytes()
+    stats = e.lastStats()
+    assert stats["rawDetections"] == len(ref)
+    assert stats["queuePasses"] == (0 if cfg["queueStumps"] == 0 else stats["queuePasses"])
+
+
+def test_bad_config_rejected(cuda, vj, basic_pool, full_case):
+    st, sg, _, _ = full_case
+    e = engine(vj, basic_pool, st, sg)
+    assert e.setConfig(tileRows=5) == vj.Status.kInvalidArg
+    assert e.setConfig(tileStumps=-1) == vj.Status.kInvalidArg
+    assert e.getConfig()["tileRows"] == 8
+
+
+def test_stats_are_consistent(cuda, vj, basic_pool, full_case):
+    st, sg, scene, ref = full_case
+    e = engine(vj, basic_pool, st, sg)
+    h, w = scene.shape
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0
+    k = e.lastStats()
+    assert k["images"] == 1 and k["levels"] > 5
+    assert k["windows"] >= k["gated"] > 0
+    assert k["stumpEvals"] >= k["gated"]
+    assert k["rawDetections"] == len(raw) == len(ref)
+    assert k["attempts"] >= 1 and k["gpuMs"] > 0
+    assert all(v >= 0 for v in k["phaseMs"].values())
+    assert k["deepWindows"] >= k["rawDetections"]
+
+
+def test_small_capacity_grows_and_repeats(cuda, vj, basic_pool, full_case):
+    """maxDetections 20 starts the per-image buffer at 64 entries; the
+    overflow is seen, the buffer grows and the launch repeats, and the result
+    is the oracle's list truncated to 20."""
+    st, sg, scene, ref = full_case
+    assert len(ref) > 64
+    e = engine(vj, basic_pool, st, sg, maxdet=20)
+    h, w = scene.shape
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 20, applyGrouping=False)
+    assert s == 0 and e.lastStats()["attempts"] >= 2
+    assert raw.tobytes() == ref[:20].tobytes()
+
+
+def test_autotune_keeps_identical_results(cuda, vj, basic_pool, full_case):
+    st, sg, scene, ref = full_case
+    e = engine(vj, basic_pool, st, sg)
+    scenes = [scene, vj.synth_scene(8, 640, 480, 4, 24, 200), vj.synth_scene(9, 320, 240, 2, 24, 100)]
+    s, cfg, ms = e.autotune(scenes, repeats=1)
+    assert s == 0 and ms > 0
+    assert cfg["tileRows"] in (4, 8, 16) and cfg == e.getConfig()
+    h, w = scene.shape
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0 and raw.tobytes() == ref.tobytes()
+
+
+def test_batch_on_device_images(cuda, vj, basic_pool, full_case):
+    torch = cuda
+    st, sg, scene, ref = full_case
+    e = engine(vj, basic_pool, st, sg)
+    others = [vj.synth_scene(20 + k, 200 + 97 * k, 150 + 61 * k, 2, 24, 120) for k in range(5)]
+    imgs = [scene] + others
+    dev = [torch.from_numpy(im).cuda() for im in imgs]
+    s, host_res = e.detectBatch(imgs, applyGrouping=False, capPerImage=20000)
+    s2, dev_res = e.detectBatch(dev, applyGrouping=False, capPerImage=20000)
+    assert s == 0 and s2 == 0
+    assert host_res[0].tobytes() == ref.tobytes()
+    for a, b in zip(host_res, dev_res):
+        assert a.tobytes() == b.tobytes()
