@@ -27,7 +27,8 @@ from . import _capi
 from ._capi import (DETECTION, FEATURE_BEST, HAAR_FEATURE, STAGE, STAGE_CALIB, STUMP4, TILE_BEST, WEAK,
                     VJError, call, load, ptr)
 
-__all__ = ["Status", "FeatureMode", "FaceVisionEngine", "AdaBoostTrainer", "ModelIO", "VJError",
+__all__ = ["Status", "FeatureMode", "FaceVisionEngine", "AdaBoostTrainer", "ModelIO", "VJError", "DetectServer",
+           "estimate_detect_bytes",
            "HAAR_FEATURE", "STUMP4", "STAGE", "DETECTION", "TILE_BEST", "WEAK", "FEATURE_BEST",
            "STAGE_CALIB", "synth_patches", "synth_scene", "synth_cascade", "feature_pool", "load"]
 
@@ -220,6 +221,15 @@ class FaceVisionEngine:
         out["hostMs"] = dict(zip(_capi.HOST_PHASES, [float(x) for x in rec["hostMs"][0]]))
         return out
 
+    def reserve(self, nbytes: int) -> int:
+        """Lays out every batch inside one device arena of nbytes (0 = grow on demand)."""
+        return Status(_capi.status("vj_detector_reserve", self._h, int(nbytes)))
+
+    def deviceBytes(self) -> int:
+        b = C.c_int64()
+        call("vj_detector_device_bytes", self._h, C.byref(b))
+        return b.value
+
     def getConfig(self) -> dict:
         rec = np.zeros(1, dtype=_capi.DETECT_CONFIG)
         call("vj_detector_get_config", self._h, ptr(rec))
@@ -246,6 +256,74 @@ class FaceVisionEngine:
         st = _capi.status("vj_detector_autotune", self._h, n, ptrs, ws, hs, ws, int(on_dev), C.c_float(scaleFactor),
                           minObjectSize, repeats, ptr(rec), C.byref(ms))
         return Status(st), {k: int(rec[k][0]) for k in _capi.DETECT_CONFIG.names}, ms.value
+
+
+def estimate_detect_bytes(w: int, h: int, scaleFactor: float = 1.25, minObjectSize: int = 24,
+                          maxDetections: int = 200000, win=(24, 24)) -> int:
+    """Device bytes one w x h image adds to a detection batch (admission estimate)."""
+    b = C.c_int64()
+    call("vj_detect_estimate_bytes", int(win[0]), int(win[1]), int(w), int(h), C.c_float(scaleFactor),
+         minObjectSize, maxDetections, C.byref(b))
+    return b.value
+
+
+class DetectServer:
+    """Continuous-batching detection server (vj_server_*): submit host images as
+    they arrive, wait for each ticket's detections."""
+
+    def __init__(self, features, stumps, stages, workers: int = 2, maxBatchImages: int = 64,
+                 hbmBudgetBytes: int = 16 << 30, maxImage=(3840, 2160), scaleFactor: float = 1.25,
+                 minNeighbors: int = 4, minObjectSize: int = 24, maxDetections: int = 200000,
+                 applyGrouping: bool = True, blocksPerSM: int = 0, tileRows: int = 0, tileStumps: int = 0,
+                 win=(24, 24)):
+        cfg = np.zeros(1, dtype=_capi.SERVER_CONFIG)
+        for k, v in dict(winW=win[0], winH=win[1], maxImageW=maxImage[0], maxImageH=maxImage[1], workers=workers,
+                         maxBatchImages=maxBatchImages, hbmBudgetBytes=hbmBudgetBytes, scaleFactor=scaleFactor,
+                         minNeighbors=minNeighbors, minObjectSize=minObjectSize, maxDetections=maxDetections,
+                         applyGrouping=int(applyGrouping), blocksPerSM=blocksPerSM, tileRows=tileRows,
+                         tileStumps=tileStumps).items():
+            cfg[k] = v
+        self._keep = [np.ascontiguousarray(a) for a in (features, stumps, stages)]
+        f, s, g = self._keep
+        h = C.c_void_p()
+        call("vj_server_create", ptr(cfg), ptr(f), len(f), ptr(s), len(s), ptr(g), len(g), C.byref(h))
+        self._h = h
+
+    def submit(self, image: np.ndarray) -> int:
+        img = np.ascontiguousarray(image, dtype=np.uint8)
+        t = C.c_uint64()
+        call("vj_server_submit", self._h, ptr(img), int(img.shape[1]), int(img.shape[0]), int(img.shape[1]),
+             C.byref(t))
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int()
+        call("vj_server_poll", self._h, C.c_uint64(ticket), C.byref(d))
+        return bool(d.value)
+
+    def wait(self, ticket: int, timeoutMs: int = -1, capacity: int = 4096):
+        """Returns (status, detections) and releases the ticket (unless it timed out)."""
+        out = np.zeros(capacity, dtype=DETECTION)
+        n = C.c_int()
+        st = _capi.status("vj_server_wait", self._h, C.c_uint64(ticket), timeoutMs, ptr(out), capacity, C.byref(n))
+        return Status(st), out[: n.value].copy()
+
+    def stats(self) -> dict:
+        rec = np.zeros(1, dtype=_capi.SERVER_STATS)
+        call("vj_server_get_stats", self._h, ptr(rec))
+        return {k: rec[k][0].item() for k in _capi.SERVER_STATS.names}
+
+    def resetStats(self) -> None:
+        call("vj_server_reset_stats", self._h)
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h:
+            _capi.status("vj_server_destroy", h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 class AdaBoostTrainer:

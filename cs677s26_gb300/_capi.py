@@ -41,10 +41,20 @@ DETECT_STATS = np.dtype([("images", "<i8"), ("levels", "<i8"), ("pyramidPixels",
                          ("attempts", "<i4"), ("queuePasses", "<i4"), ("gpuMs", "<f8"), ("phaseMs", "<f8", 6),
                          ("hostMs", "<f8", 3)])
 DETECT_CONFIG = np.dtype([("tileRows", "<i4"), ("tileStumps", "<i4"), ("queueStumps", "<i4"), ("blocksPerSM", "<i4")])
+SERVER_CONFIG = np.dtype([("winW", "<i4"), ("winH", "<i4"), ("maxImageW", "<i4"), ("maxImageH", "<i4"),
+                          ("workers", "<i4"), ("maxBatchImages", "<i4"), ("hbmBudgetBytes", "<i8"),
+                          ("scaleFactor", "<f4"), ("minNeighbors", "<i4"), ("minObjectSize", "<i4"),
+                          ("maxDetections", "<i4"), ("applyGrouping", "<i4"), ("blocksPerSM", "<i4"),
+                          ("tileRows", "<i4"), ("tileStumps", "<i4")])
+SERVER_STATS = np.dtype([("submitted", "<i8"), ("completed", "<i8"), ("failed", "<i8"), ("batches", "<i8"),
+                         ("meanBatchImages", "<f8"), ("meanMs", "<f8"), ("p50Ms", "<f8"), ("p99Ms", "<f8"),
+                         ("p999Ms", "<f8"), ("maxMs", "<f8"), ("elapsedS", "<f8"), ("imagesPerS", "<f8"),
+                         ("peakAdmittedBytes", "<i8"), ("deviceBytes", "<i8")])
 PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "compaction")
 HOST_PHASES = ("plan_upload", "wait", "sort_group")
 
 assert DETECT_STATS.itemsize == 152 and DETECT_CONFIG.itemsize == 16
+assert SERVER_CONFIG.itemsize == 64 and SERVER_STATS.itemsize == 112
 assert HAAR_FEATURE.itemsize == 64 and STUMP4.itemsize == 16 and STAGE.itemsize == 12
 assert DETECTION.itemsize == 24 and TILE_BEST.itemsize == 16 and WEAK.itemsize == 28
 
@@ -97,6 +107,17 @@ SIGNATURES = {
     "vj_detector_set_config": (i32, [vp, vp]),
     "vj_detector_get_config": (i32, [vp, vp]),
     "vj_detector_autotune": (i32, [vp, i32, vp, vp, vp, vp, i32, f32, i32, i32, vp, vp]),
+    "vj_detector_reserve": (i32, [vp, i64]),
+    "vj_detector_occupancy": (i32, [vp, pi32]),
+    "vj_detector_device_bytes": (i32, [vp, pi64]),
+    "vj_detect_estimate_bytes": (i32, [i32, i32, i32, i32, f32, i32, i32, pi64]),
+    "vj_server_create": (i32, [vp, vp, i64, vp, i64, vp, i64, C.POINTER(vp)]),
+    "vj_server_submit": (i32, [vp, vp, i32, i32, i32, C.POINTER(C.c_uint64)]),
+    "vj_server_poll": (i32, [vp, u64, pi32]),
+    "vj_server_wait": (i32, [vp, u64, i32, vp, i32, pi32]),
+    "vj_server_get_stats": (i32, [vp, vp]),
+    "vj_server_reset_stats": (i32, [vp]),
+    "vj_server_destroy": (i32, [vp]),
     "vj_synth_patches": (i32, [u64, i32, i32, vp]),
     "vj_synth_scene": (i32, [u64, i32, i32, i32, i32, i32, vp]),
     "vj_synth_cascade": (i32, [u64, i32, i32, vp, vp]),

@@ -26,18 +26,21 @@ struct alignas(16) DStump {
 };
 static_assert(sizeof(DStump) == 64, "DStump is 64 bytes");
 
-// Stump record for the warp-per-window deep pass: corner offsets into the
-// window's (winW+1) x (winH+1) integral patch, which are the feature's own
-// p0..p3 indices (FastRect, common_types.cuh:26-35).  A 2-rectangle feature
-// has w2 == 0 and its third rectangle is not evaluated; for a 3-rectangle
-// feature with w2 == 0 skipping it is also exact, because adding the signed
-// zero v2 can only flip the sign of a zero raw, which compares equal.
-struct alignas(16) PStump {
-    float theta, left, right, w0;
-    float w1, w2;
-    uint32_t o[6];  // offsets 2k (low half) and 2k+1 (high half) of corners 0..11
+// Stump record for the warp-per-window deep pass, stored as three 16-byte
+// planes (structure of arrays) so that lanes reading consecutive stumps read
+// consecutive 16-byte words:
+//   A = {theta, left, right, w0}, B = {w1, w2, o01, o23}, C = {o45, o67, o89, o1011}
+// where oXY packs the offsets of corners X (low half) and Y (high half) into
+// the window's (winW+1) x (winH+1) integral patch - the feature's own p0..p3
+// indices (FastRect, common_types.cuh:26-35).  A 2-rectangle feature has
+// w2 == 0 and its third rectangle is not evaluated; for a 3-rectangle feature
+// with w2 == 0 skipping it is also exact, because adding the signed zero v2
+// can only flip the sign of a zero raw, which compares equal.
+struct PStumpPlanes {
+    const uint4* a;
+    const uint4* b;
+    const uint4* c;
 };
-static_assert(sizeof(PStump) == 48, "PStump is 48 bytes");
 
 struct DStage {
     int32_t first, ntrees;
@@ -119,7 +122,7 @@ struct DevPlan {
     uint32_t* totS;
     uint64_t* totQ;
     const DStump* stumps;
-    const PStump* pstumps;
+    PStumpPlanes pstumps;
     const DStage* stages;
     QEntry* q[2];
     vj_detection* dets;         // nImg * detCap, image i at dets + i * detCap
@@ -312,12 +315,12 @@ __device__ __forceinline__ float stage_sum(const DStump* __restrict__ stumps, co
     return acc;
 }
 
-// Leaf value of one stump from the window's integral patch in shared memory
+// Leaf value of stump k from the window's integral patch in shared memory
 // (corners already converted to float).
-__device__ __forceinline__ float patch_stump_value(const PStump* __restrict__ sp, const float* patch, float inv) {
-    const float4 a = __ldg(reinterpret_cast<const float4*>(sp));
-    const uint4 b = __ldg(reinterpret_cast<const uint4*>(sp) + 1);
-    const uint4 c = __ldg(reinterpret_cast<const uint4*>(sp) + 2);
+__device__ __forceinline__ float patch_stump_value(const PStumpPlanes& ps, int k, const float* patch, float inv) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(ps.a + k));
+    const uint4 b = __ldg(ps.b + k);
+    const uint4 c = __ldg(ps.c + k);
     const float w1 = __uint_as_float(b.x), w2 = __uint_as_float(b.y);
     const float v0 = __fmul_rn(
         __fadd_rn(__fsub_rn(__fsub_rn(patch[b.z & 0xFFFFu], patch[b.z >> 16]), patch[b.w & 0xFFFFu]), patch[b.w >> 16]),
@@ -525,12 +528,11 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* patch, const 
             bool alive = true;
             for (int si = P.deepFrom; si < P.nStages; ++si) {
                 const DStage st = P.stages[si];
-                const PStump* sp = P.pstumps + st.first;
                 float acc = 0.0f;
                 for (int k0 = 0; k0 < st.ntrees; k0 += 32) {
                     const int k = k0 + lane;
                     float c = 0.0f;
-                    if (k < st.ntrees) c = patch_stump_value(sp + k, patch, e.inv);
+                    if (k < st.ntrees) c = patch_stump_value(P.pstumps, st.first + k, patch, e.inv);
                     const int m = min(32, st.ntrees - k0);
                     if (m == 32) {
 #pragma unroll
@@ -567,8 +569,8 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* patch, const 
 //   6. compaction of the raw detections, image after image, into the
 //      host-mapped buffer.
 // ---------------------------------------------------------------------------
-template <int TH>
-__global__ void __launch_bounds__(kCasThreads)
+template <int TH, int MINB>
+__global__ void __launch_bounds__(kCasThreads, MINB)
 detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     extern __shared__ __align__(16) unsigned char dsmem[];
     const DevPlan& P = *plan;

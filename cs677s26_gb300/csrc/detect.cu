@@ -23,16 +23,21 @@
 #include <vector>
 
 #include "cascade.cuh"
+#include "group.h"
 
 namespace vjgb {
 namespace {
 
+// Device buffer: owned and grown on demand, or (view) a fixed range of the
+// detector's arena, which never grows.
 struct DBuf {
     void* p = nullptr;
     size_t cap = 0;
+    bool view = false;
     // Grows to at least `bytes`; returns VJ_OK.  Contents are not kept.
     int ensure(size_t bytes) {
         if (bytes <= cap && p) return VJ_OK;
+        if (view) return set_error(VJ_OUT_OF_MEMORY, "detector arena: batch does not fit the reserved bytes");
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
@@ -47,9 +52,16 @@ struct DBuf {
         return VJ_OK;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p && !view) cudaFree(p);
         p = nullptr;
         cap = 0;
+        view = false;
+    }
+    void set_view(void* base, size_t bytes) {
+        release();
+        p = base;
+        cap = bytes;
+        view = true;
     }
     template <class T>
     T* as() const { return static_cast<T*>(p); }
@@ -149,116 +161,6 @@ bool canonical_less(const vj_detection& a, const vj_detection& b) {
 
 }  // namespace
 
-// Restatement of groupRectanglesCpu (face_vision_engine.cu:1401-1539):
-// union-find (path compression, union by rank) over similar rectangles found
-// by an x-sorted sweep, clusters with more than max(1, minNeighbors) members
-// averaged with integer division, then clusters contained in a more populous
-// one dropped.
-std::vector<vj_detection> group_rectangles(const std::vector<vj_detection>& in, int minNeighbors, float eps) {
-    const int n = static_cast<int>(in.size());
-    if (n == 0) return {};
-    std::vector<int> parent(n), rnk(n, 0), order(n);
-    for (int i = 0; i < n; ++i) parent[i] = order[i] = i;
-    auto find = [&](int x) {
-        int r = x;
-        while (parent[r] != r) r = parent[r];
-        while (parent[x] != r) {
-            const int nx = parent[x];
-            parent[x] = r;
-            x = nx;
-        }
-        return r;
-    };
-    auto unite = [&](int a, int b) {
-        a = find(a);
-        b = find(b);
-        if (a == b) return;
-        if (rnk[a] < rnk[b]) std::swap(a, b);
-        parent[b] = a;
-        if (rnk[a] == rnk[b]) ++rnk[a];
-    };
-    auto byX = [](const std::vector<vj_detection>& v) {
-        return [&v](int a, int b) { return v[a].x != v[b].x ? v[a].x < v[b].x : a < b; };
-    };
-    std::sort(order.begin(), order.end(), byX(in));
-    for (int oi = 0; oi < n; ++oi) {
-        const vj_detection& a = in[order[oi]];
-        const int reach = static_cast<int>(eps * static_cast<float>(a.w + a.h) * 0.5f);
-        for (int oj = oi + 1; oj < n; ++oj) {
-            const vj_detection& b = in[order[oj]];
-            if (b.x - a.x > reach) break;
-            const int delta = static_cast<int>(eps * static_cast<float>(std::min(a.w, b.w) + std::min(a.h, b.h)) * 0.5f);
-            if (std::abs(a.x - b.x) <= delta && std::abs(a.y - b.y) <= delta &&
-                std::abs(a.x + a.w - b.x - b.w) <= delta && std::abs(a.y + a.h - b.y - b.h) <= delta)
-                unite(order[oi], order[oj]);
-        }
-    }
-    struct Acc {
-        int64_t x = 0, y = 0, w = 0, h = 0;
-        int count = 0;
-        float best = -INFINITY;
-        int scaleIdx = 0;
-    };
-    std::vector<Acc> acc(n);
-    for (int i = 0; i < n; ++i) {
-        Acc& c = acc[find(i)];
-        c.x += in[i].x;
-        c.y += in[i].y;
-        c.w += in[i].w;
-        c.h += in[i].h;
-        c.count += 1;
-        if (in[i].score > c.best) {
-            c.best = in[i].score;
-            c.scaleIdx = in[i].scaleIdx;
-        }
-    }
-    std::vector<vj_detection> cl;
-    std::vector<int> cc;
-    const int minN = std::max(1, minNeighbors);
-    for (int i = 0; i < n; ++i) {
-        if (find(i) != i || acc[i].count <= minN) continue;
-        const Acc& c = acc[i];
-        vj_detection d;
-        d.x = static_cast<int>(c.x / c.count);
-        d.y = static_cast<int>(c.y / c.count);
-        d.w = static_cast<int>(c.w / c.count);
-        d.h = static_cast<int>(c.h / c.count);
-        d.scaleIdx = c.scaleIdx;
-        d.score = c.best;
-        cl.push_back(d);
-        cc.push_back(c.count);
-    }
-    int maxW = 0;
-    for (const auto& d : cl) maxW = std::max(maxW, d.w);
-    std::vector<int> co(cl.size());
-    for (size_t i = 0; i < cl.size(); ++i) co[i] = static_cast<int>(i);
-    std::sort(co.begin(), co.end(), byX(cl));
-    std::vector<vj_detection> out;
-    for (size_t i = 0; i < cl.size(); ++i) {
-        const vj_detection& r1 = cl[i];
-        const int n1 = cc[i];
-        const float lb = static_cast<float>(r1.x + r1.w) - (1.0f + eps) * static_cast<float>(maxW);
-        const float rb = static_cast<float>(r1.x) + eps * static_cast<float>(maxW);
-        bool drop = false;
-        for (int o : co) {
-            const vj_detection& r2 = cl[o];
-            if (r2.x < static_cast<int>(lb)) continue;
-            if (r2.x > static_cast<int>(rb)) break;
-            if (static_cast<size_t>(o) == i) continue;
-            const int n2 = cc[o];
-            const int dx = static_cast<int>(static_cast<float>(r2.w) * eps);
-            const int dy = static_cast<int>(static_cast<float>(r2.h) * eps);
-            if (r1.x >= r2.x - dx && r1.y >= r2.y - dy && r1.x + r1.w <= r2.x + r2.w + dx &&
-                r1.y + r1.h <= r2.y + r2.h + dy && (n2 > std::max(3, n1) || n1 < 3)) {
-                drop = true;
-                break;
-            }
-        }
-        if (!drop) out.push_back(r1);
-    }
-    return out;
-}
-
 }  // namespace vjgb
 
 using namespace vjgb;
@@ -268,11 +170,14 @@ struct vj_detector {
     int normMode = VJ_NORM_FLOAT_CORNERS;
     int nStages = 0, nStumps = 0;
     std::vector<DStage> hStages;
-    DBuf stumps, pstumps, stages;
+    DBuf stumps, pstumps, stages;  // pstumps: planes A, B, C of nStumps uint4 each
     // Work buffers, grown on demand.
     DBuf imgs, pix, iiSum, iiSq, totS, totQ, qA, qB, dets, dplan, dctrl;
     HBuf hplan, hctrl, hdets;
     int imageCap = 0;  // images the control block has room for
+    // Optional arena (vj_detector_reserve): every work buffer of a batch is a
+    // range of it, so the detector never holds more than its reservation.
+    DBuf arena;
     // Launch shape and the stage schedule derived from it.
     vj_detect_config cfg{8, 64, 0, 0};
     int tileStages = 0, deepFrom = 0;
@@ -332,15 +237,20 @@ void schedule_passes(vj_detector* d) {
 }
 
 template <int TH>
-const void* kernel_for() {
-    return reinterpret_cast<const void*>(&detect_persistent_kernel<TH>);
+const void* kernel_for(int blocksPerSM) {
+    if (blocksPerSM >= 4) return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 4>);
+    if (blocksPerSM == 1 || blocksPerSM == 2) return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 2>);
+    return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 3>);
 }
 
-const void* kernel_ptr(int th) {
+// Kernel variant for a launch shape: tile rows, and the residency the kernel
+// is compiled for - 2, 3 (also for blocksPerSM 0) or 4 CTAs of 256 threads
+// per SM, which caps its registers at 128, 85 or 64.
+const void* kernel_ptr(int th, int blocksPerSM) {
     switch (th) {
-        case 4: return kernel_for<4>();
-        case 16: return kernel_for<16>();
-        default: return kernel_for<8>();
+        case 4: return kernel_for<4>(blocksPerSM);
+        case 16: return kernel_for<16>(blocksPerSM);
+        default: return kernel_for<8>(blocksPerSM);
     }
 }
 
@@ -360,7 +270,7 @@ int ensure_graph(vj_detector* d, size_t planBytes) {
     const int th = d->cfg.tileRows;
     const size_t smem = smem_bytes(d, th);
     const size_t cbytes = ctrl_bytes(d->imageCap);
-    const void* fn = kernel_ptr(th);
+    const void* fn = kernel_ptr(th, d->cfg.blocksPerSM);
     VJ_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int fit = 0;
     VJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, kCasThreads, smem));
@@ -450,11 +360,66 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             iiElems += (g.h + 1) * ii_pitch(g.w);
         }
     }
-    int st;
-    if (!onDevice && (st = D->imgs.ensure(imgBytes)) != VJ_OK) return st;
-    if ((st = D->pix.ensure(pixBytes)) != VJ_OK) return st;
-    if ((st = D->iiSum.ensure(iiElems * 4)) != VJ_OK) return st;
-    if ((st = D->iiSq.ensure(iiElems * 8)) != VJ_OK) return st;
+    int64_t totRows = 0, totPitch = 0, windowsAll = 0;
+    for (int i = 0; i < nImg; ++i)
+        for (const auto& g : geo[i]) {
+            totRows += col_segs(g.h);
+            totPitch = std::max<int64_t>(totPitch, static_cast<int64_t>(col_chunks(g.w)) * 32);
+            windowsAll += static_cast<int64_t>((g.w - D->winW + g.step) / g.step) * ((g.h - D->winH + g.step) / g.step);
+        }
+    const int64_t totElems = std::max<int64_t>(1, totRows * totPitch);
+    int64_t qcap = std::min<int64_t>(std::max<int64_t>({windowsAll / 8, int64_t(1) << 16, D->qHint}), INT32_MAX / 2);
+    int detCap = std::max({64, std::min(D->maxDet, 4096), D->detHint});
+    // Work buffers: grown on demand, or carved from the arena with the queues
+    // taking whatever the other buffers leave.
+    auto layout = [&]() -> int {
+        const size_t detBytes = sizeof(vj_detection) * static_cast<size_t>(detCap) * nImg;
+        if (!D->arena.p) {
+            int r;
+            if (!onDevice && (r = D->imgs.ensure(imgBytes)) != VJ_OK) return r;
+            if ((r = D->pix.ensure(pixBytes)) != VJ_OK) return r;
+            if ((r = D->iiSum.ensure(iiElems * 4)) != VJ_OK) return r;
+            if ((r = D->iiSq.ensure(iiElems * 8)) != VJ_OK) return r;
+            if ((r = D->totS.ensure(totElems * 4)) != VJ_OK) return r;
+            if ((r = D->totQ.ensure(totElems * 8)) != VJ_OK) return r;
+            if ((r = D->dets.ensure(detBytes)) != VJ_OK) return r;
+            if ((r = D->qA.ensure(sizeof(QEntry) * static_cast<size_t>(qcap))) != VJ_OK) return r;
+            return D->qB.ensure(sizeof(QEntry) * static_cast<size_t>(qcap));
+        }
+        char* base = D->arena.as<char>();
+        size_t off = 0;
+        const size_t cap = D->arena.cap;
+        bool fits = true;
+        auto carve = [&](DBuf& b, size_t bytes) {
+            off = static_cast<size_t>(align_up(static_cast<int64_t>(off), 256));
+            bytes = std::max<size_t>(bytes, 256);
+            if (off + bytes > cap) {
+                fits = false;
+                return;
+            }
+            b.set_view(base + off, bytes);
+            off += bytes;
+        };
+        carve(D->imgs, static_cast<size_t>(imgBytes));
+        carve(D->pix, static_cast<size_t>(pixBytes));
+        carve(D->iiSum, static_cast<size_t>(iiElems) * 4);
+        carve(D->iiSq, static_cast<size_t>(iiElems) * 8);
+        carve(D->totS, static_cast<size_t>(totElems) * 4);
+        carve(D->totQ, static_cast<size_t>(totElems) * 8);
+        carve(D->dets, detBytes);
+        off = static_cast<size_t>(align_up(static_cast<int64_t>(off), 256));
+        const int64_t room = fits && off < cap ? static_cast<int64_t>((cap - off) / 2 / sizeof(QEntry)) - 32 : 0;
+        const int64_t q = std::min<int64_t>(room, INT32_MAX / 2);
+        if (!fits || q < std::max<int64_t>(windowsAll / 8, 1))
+            return set_error(VJ_OUT_OF_MEMORY, "detector arena: " + std::to_string(cap) +
+                                                   " reserved bytes do not hold this batch");
+        qcap = q;
+        carve(D->qA, sizeof(QEntry) * static_cast<size_t>(qcap));
+        carve(D->qB, sizeof(QEntry) * static_cast<size_t>(qcap));
+        return fits ? VJ_OK : set_error(VJ_OUT_OF_MEMORY, "detector arena: queues do not fit");
+    };
+    int st = layout();
+    if (st != VJ_OK) return st;
 
     std::vector<IIJob> iij;
     std::vector<CasLevel> lv;
@@ -526,8 +491,6 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         }
     }
     const IIPlan ip = plan_integral_jobs(iij.data(), static_cast<int>(iij.size()));
-    if ((st = D->totS.ensure(std::max<int64_t>(1, ip.totRows * ip.totPitch) * 4)) != VJ_OK) return st;
-    if ((st = D->totQ.ensure(std::max<int64_t>(1, ip.totRows * ip.totPitch) * 8)) != VJ_OK) return st;
 
     // ---- plan bytes: [DevPlan][rjFirst][rjItems][ResizeJob...][IIJob...][CasLevel...]
     const int nResize = static_cast<int>(rj.size());
@@ -577,17 +540,13 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     S.windows = windows;
     S.queuePasses = static_cast<int>(D->queueEnds.size());
 
-    int64_t qcap = std::min<int64_t>(std::max<int64_t>({windows / 8, int64_t(1) << 16, D->qHint}), INT32_MAX / 2);
-    int detCap = std::max({64, std::min(D->maxDet, 4096), D->detHint});
     int64_t hostCap = std::max<int64_t>({int64_t(1) << 16, D->hostHint});
     if (!D->ev0) {
         VJ_CUDA_TRY(cudaEventCreate(&D->ev0));
         VJ_CUDA_TRY(cudaEventCreate(&D->ev1));
     }
     for (int attempt = 0; attempt < 4; ++attempt) {
-        if ((st = D->dets.ensure(sizeof(vj_detection) * static_cast<size_t>(detCap) * nImg)) != VJ_OK) return st;
-        if ((st = D->qA.ensure(sizeof(QEntry) * static_cast<size_t>(qcap))) != VJ_OK) return st;
-        if ((st = D->qB.ensure(sizeof(QEntry) * static_cast<size_t>(qcap))) != VJ_OK) return st;
+        if (attempt > 0 && (st = layout()) != VJ_OK) return st;
         if ((st = D->hdets.ensure(sizeof(vj_detection) * static_cast<size_t>(hostCap), true)) != VJ_OK) return st;
         DevPlan P{};
         P.nImg = nImg;
@@ -614,7 +573,9 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         P.totS = D->totS.as<uint32_t>();
         P.totQ = D->totQ.as<uint64_t>();
         P.stumps = D->stumps.as<DStump>();
-        P.pstumps = D->pstumps.as<PStump>();
+        P.pstumps.a = D->pstumps.as<uint4>();
+        P.pstumps.b = P.pstumps.a + D->nStumps;
+        P.pstumps.c = P.pstumps.b + D->nStumps;
         P.stages = D->stages.as<DStage>();
         P.q[0] = D->qA.as<QEntry>();
         P.q[1] = D->qB.as<QEntry>();
@@ -695,7 +656,7 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
     auto post = [&](int i) {
         const vj_detection* src = hd + ho[i];
         std::vector<vj_detection> raw(src, src + std::min(hc[i], detCap));
-        std::sort(raw.begin(), raw.end(), canonical_less);
+        canonical_sort(raw);
         if (static_cast<int>(raw.size()) > limit) raw.resize(limit);
         std::vector<vj_detection> res = group ? group_rectangles(raw, minN, 0.2f) : std::move(raw);
         const int k = std::min(static_cast<int>(res.size()), capPer);
@@ -761,7 +722,7 @@ int vj_detector_destroy(vj_detector* d) {
     if (d->ev0) cudaEventDestroy(d->ev0);
     if (d->ev1) cudaEventDestroy(d->ev1);
     for (DBuf* b : {&d->stumps, &d->pstumps, &d->stages, &d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS, &d->totQ,
-                    &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl})
+                    &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->arena})
         b->release();
     d->hplan.release();
     d->hctrl.release();
@@ -789,19 +750,17 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
     const int mW = d->winW + 1;
     const int patchElems = (d->winW + 1) * (d->winH + 1);
     std::vector<DStump> ds(static_cast<size_t>(stumpCount));
-    std::vector<PStump> ps(static_cast<size_t>(stumpCount));
+    std::vector<uint4> pa(static_cast<size_t>(stumpCount)), pb(pa.size()), pc(pa.size());
     for (int64_t i = 0; i < stumpCount; ++i) {
         const int32_t fi = float_bits(stumps[i].featureBits);
         if (fi < 0 || fi >= featureCount)
             return set_error(VJ_INVALID_ARG, "vj_detector_set_model: stump references a missing feature");
         const vj_haar_feature& f = features[fi];
         DStump& o = ds[static_cast<size_t>(i)];
-        PStump& q = ps[static_cast<size_t>(i)];
         std::memset(&o, 0, sizeof(o));
-        std::memset(&q, 0, sizeof(q));
-        o.theta = q.theta = stumps[i].theta;
-        o.left = q.left = stumps[i].leftVal;
-        o.right = q.right = stumps[i].rightVal;
+        o.theta = stumps[i].theta;
+        o.left = stumps[i].leftVal;
+        o.right = stumps[i].rightVal;
         o.nr = f.rectCount == 3 ? 3 : 2;
         const vj_fast_rect* rr[3] = {&f.r0, &f.r1, &f.r2};
         uint16_t off[12] = {0};
@@ -818,11 +777,15 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
                 off[4 * r + c] = static_cast<uint16_t>(r < o.nr ? p[c] : 0);
             }
         }
-        q.w0 = rr[0]->w;
-        q.w1 = rr[1]->w;
-        q.w2 = o.nr == 3 ? rr[2]->w : 0.0f;
+        uint32_t ow[6];
         for (int k = 0; k < 6; ++k)
-            q.o[k] = static_cast<uint32_t>(off[2 * k]) | (static_cast<uint32_t>(off[2 * k + 1]) << 16);
+            ow[k] = static_cast<uint32_t>(off[2 * k]) | (static_cast<uint32_t>(off[2 * k + 1]) << 16);
+        const size_t j = static_cast<size_t>(i);
+        pa[j] = make_uint4(static_cast<uint32_t>(float_bits(o.theta)), static_cast<uint32_t>(float_bits(o.left)),
+                           static_cast<uint32_t>(float_bits(o.right)), static_cast<uint32_t>(float_bits(rr[0]->w)));
+        pb[j] = make_uint4(static_cast<uint32_t>(float_bits(rr[1]->w)),
+                           static_cast<uint32_t>(float_bits(o.nr == 3 ? rr[2]->w : 0.0f)), ow[0], ow[1]);
+        pc[j] = make_uint4(ow[2], ow[3], ow[4], ow[5]);
     }
     std::vector<DStage> dst(static_cast<size_t>(stageCount));
     for (int64_t i = 0; i < stageCount; ++i) {
@@ -833,10 +796,14 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
     }
     int st;
     if ((st = d->stumps.ensure(sizeof(DStump) * ds.size())) != VJ_OK) return st;
-    if ((st = d->pstumps.ensure(sizeof(PStump) * ps.size())) != VJ_OK) return st;
+    if ((st = d->pstumps.ensure(sizeof(uint4) * 3 * pa.size())) != VJ_OK) return st;
     if ((st = d->stages.ensure(sizeof(DStage) * dst.size())) != VJ_OK) return st;
     VJ_CUDA_TRY(cudaMemcpy(d->stumps.p, ds.data(), sizeof(DStump) * ds.size(), cudaMemcpyHostToDevice));
-    VJ_CUDA_TRY(cudaMemcpy(d->pstumps.p, ps.data(), sizeof(PStump) * ps.size(), cudaMemcpyHostToDevice));
+    for (int k = 0; k < 3; ++k) {
+        const std::vector<uint4>& plane = k == 0 ? pa : (k == 1 ? pb : pc);
+        VJ_CUDA_TRY(cudaMemcpy(d->pstumps.as<uint4>() + k * pa.size(), plane.data(), sizeof(uint4) * plane.size(),
+                               cudaMemcpyHostToDevice));
+    }
     VJ_CUDA_TRY(cudaMemcpy(d->stages.p, dst.data(), sizeof(DStage) * dst.size(), cudaMemcpyHostToDevice));
     d->nStages = static_cast<int>(stageCount);
     d->nStumps = static_cast<int>(stumpCount);
@@ -864,6 +831,61 @@ int vj_detector_set_config(vj_detector* d, const vj_detect_config* cfg) {
 int vj_detector_get_config(const vj_detector* d, vj_detect_config* cfg) {
     if (!d || !cfg) return set_error(VJ_INVALID_ARG, "vj_detector_get_config: null argument");
     *cfg = d->cfg;
+    return ok();
+}
+
+int vj_detector_reserve(vj_detector* d, int64_t bytes) {
+    if (!d || bytes < 0) return set_error(VJ_INVALID_ARG, "vj_detector_reserve: bad arguments");
+    for (DBuf* b : {&d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS, &d->totQ, &d->qA, &d->qB, &d->dets}) b->release();
+    d->arena.release();
+    if (bytes == 0) return ok();
+    const cudaError_t e = cudaMalloc(&d->arena.p, static_cast<size_t>(bytes));
+    if (e != cudaSuccess) {
+        d->arena.p = nullptr;
+        return set_error(VJ_OUT_OF_MEMORY, std::string("vj_detector_reserve: ") + cudaGetErrorString(e));
+    }
+    d->arena.cap = static_cast<size_t>(bytes);
+    return ok();
+}
+
+int vj_detector_occupancy(vj_detector* d, int* blocksPerSM) {
+    if (!d || !blocksPerSM) return set_error(VJ_INVALID_ARG, "vj_detector_occupancy: null argument");
+    const int th = d->cfg.tileRows;
+    const size_t smem = smem_bytes(d, th);
+    const void* fn = kernel_ptr(th, d->cfg.blocksPerSM);
+    VJ_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int fit = 0;
+    VJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, kCasThreads, smem));
+    *blocksPerSM = fit;
+    return ok();
+}
+
+int vj_detector_device_bytes(const vj_detector* d, int64_t* bytes) {
+    if (!d || !bytes) return set_error(VJ_INVALID_ARG, "vj_detector_device_bytes: null argument");
+    int64_t t = 0;
+    for (const DBuf* b : {&d->stumps, &d->pstumps, &d->stages, &d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS,
+                          &d->totQ, &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->arena})
+        if (!b->view) t += static_cast<int64_t>(b->cap);
+    *bytes = t;
+    return ok();
+}
+
+int vj_detect_estimate_bytes(int winW, int winH, int w, int h, float scaleFactor, int minObjectSize,
+                             int maxDetections, int64_t* bytes) {
+    if (!bytes || winW < 3 || winH < 3 || w <= 0 || h <= 0 || !(scaleFactor > 1.0f) || minObjectSize < 1)
+        return set_error(VJ_INVALID_ARG, "vj_detect_estimate_bytes: bad arguments");
+    int64_t t = align_up(w, 16) * h;  // image copy
+    for (const LevelGeom& g : plan_levels(w, h, winW, winH, scaleFactor, minObjectSize)) {
+        if (g.src != -2) t += align_up(g.w, 16) * g.h;           // resized level
+        const int64_t ii = static_cast<int64_t>(g.h + 1) * ii_pitch(g.w);
+        t += ii * 12;                                              // sums + squared sums
+        t += static_cast<int64_t>(col_segs(g.h)) * col_chunks(g.w) * 32 * 12;  // segment totals
+        const int64_t win = static_cast<int64_t>((g.w - winW + g.step) / g.step) * ((g.h - winH + g.step) / g.step);
+        t += 2 * static_cast<int64_t>(sizeof(QEntry)) * (win / 8 + 1);        // two queues
+        t += static_cast<int64_t>(sizeof(CasLevel) + sizeof(IIJob) + sizeof(ResizeJob));
+    }
+    t += static_cast<int64_t>(sizeof(vj_detection)) * std::max(64, std::min(std::max(1, maxDetections), 4096));
+    *bytes = t + t / 8;  // the work buffers grow with an eighth of slack
     return ok();
 }
 
@@ -934,60 +956,76 @@ int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images, co
         acc += d->hStages[s].ntrees;
         depths.push_back(acc);
     }
-    std::vector<vj_detect_config> cands;
-    for (int th : {8, 4, 16})
-        for (int dep : depths) cands.push_back(vj_detect_config{th, dep, 0, 0});
+    // Two rounds: first the tile shape and residency at the current tile-pass
+    // depth, then the depth with the best of those.  Every candidate's raw
+    // detections must equal the first candidate's.
     const vj_detect_config saved = d->cfg;
     std::vector<std::vector<vj_detection>> ref;
     double bestMs = 0.0;
-    int best = -1;
-    for (size_t c = 0; c < cands.size() && st == VJ_OK; ++c) {
-        d->cfg = cands[c];
+    vj_detect_config bestCfg = saved;
+    bool have = false;
+    auto trial = [&](const vj_detect_config& cand) -> int {
+        d->cfg = cand;
         schedule_passes(d);
         const int* hc = nullptr;
         const int* ho = nullptr;
         int detCap = 0;
-        st = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, nullptr, &hc, &ho, &detCap);
-        if (st != VJ_OK) break;
-        // every candidate must give the same raw detections as the first
+        int r = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, nullptr, &hc, &ho, &detCap);
+        if (r != VJ_OK) return r;
         std::vector<std::vector<vj_detection>> got(static_cast<size_t>(n));
         const vj_detection* hd = d->hdets.as<vj_detection>();
         for (int i = 0; i < n; ++i) {
             got[i].assign(hd + ho[i], hd + ho[i] + std::min(hc[i], detCap));
             std::sort(got[i].begin(), got[i].end(), canonical_less);
         }
-        if (c == 0) {
+        if (ref.empty()) {
             ref = std::move(got);
         } else {
             for (int i = 0; i < n; ++i)
                 if (got[i].size() != ref[i].size() ||
                     (!got[i].empty() &&
-                     std::memcmp(got[i].data(), ref[i].data(), sizeof(vj_detection) * got[i].size()) != 0)) {
-                    d->cfg = saved;
-                    schedule_passes(d);
+                     std::memcmp(got[i].data(), ref[i].data(), sizeof(vj_detection) * got[i].size()) != 0))
                     return set_error(VJ_RUNTIME_ERROR,
                                      "vj_detector_autotune: configurations disagree on image " + std::to_string(i));
-                }
         }
         std::vector<double> t;
-        for (int r = 0; r < repeats && st == VJ_OK; ++r) {
-            st = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, nullptr, &hc, &ho, &detCap);
+        for (int k = 0; k < repeats; ++k) {
+            r = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, nullptr, &hc, &ho, &detCap);
+            if (r != VJ_OK) return r;
             t.push_back(d->stats.gpuMs);
         }
-        if (st != VJ_OK) break;
         std::sort(t.begin(), t.end());
         const double med = t[t.size() / 2];
-        if (best < 0 || med < bestMs) {
-            best = static_cast<int>(c);
+        if (!have || med < bestMs) {
+            have = true;
             bestMs = med;
+            bestCfg = cand;
         }
+        return VJ_OK;
+    };
+    for (int th : {8, 4, 16})
+        for (int bps : {0, 4, 2}) {
+            if (st != VJ_OK) break;
+            vj_detect_config c = saved;
+            c.tileRows = th;
+            c.blocksPerSM = bps;
+            c.queueStumps = 0;
+            st = trial(c);
+        }
+    const vj_detect_config shape = bestCfg;
+    for (int dep : depths) {
+        if (st != VJ_OK) break;
+        vj_detect_config c = shape;
+        c.tileStumps = dep;
+        st = trial(c);
     }
+    const int best = have ? 0 : -1;
     if (st != VJ_OK || best < 0) {
         d->cfg = saved;
         schedule_passes(d);
         return st != VJ_OK ? st : set_error(VJ_RUNTIME_ERROR, "vj_detector_autotune: no candidate ran");
     }
-    d->cfg = cands[static_cast<size_t>(best)];
+    d->cfg = bestCfg;
     schedule_passes(d);
     if (chosen) *chosen = d->cfg;
     if (chosenMs) *chosenMs = bestMs;

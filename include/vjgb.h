@@ -426,6 +426,26 @@ typedef struct vj_detect_config {
 int vj_detector_set_config(vj_detector* d, const vj_detect_config* cfg);
 int vj_detector_get_config(const vj_detector* d, vj_detect_config* cfg);
 
+/* Reserves one device arena of `bytes` for the detector's work buffers (0 =
+ * back to buffers grown on demand).  Every batch is then laid out inside it,
+ * the queues taking what the other buffers leave; a batch that does not fit
+ * returns VJ_OUT_OF_MEMORY.  The serving loop reserves each worker's share of
+ * its HBM budget this way. */
+int vj_detector_reserve(vj_detector* d, int64_t bytes);
+
+/* CTAs per SM the detection kernel can keep resident with the current
+ * config's tile rows (the ceiling for blocksPerSM). */
+int vj_detector_occupancy(vj_detector* d, int* blocksPerSM);
+
+/* Device bytes the detector's work buffers hold now. */
+int vj_detector_device_bytes(const vj_detector* d, int64_t* bytes);
+
+/* Upper estimate of the device bytes one w x h image adds to a batch
+ * (image copy, pyramid levels, integral images, queue and detection space);
+ * the serving loop admits requests against its HBM budget with it. */
+int vj_detect_estimate_bytes(int winW, int winH, int w, int h, float scaleFactor,
+                             int minObjectSize, int maxDetections, int64_t* bytes);
+
 /* Autotuner: runs every candidate configuration on the given images
  * (vj_detect_batch arguments, without grouping), `repeats` timed launches
  * each, checks that each candidate's raw detections equal the first
@@ -435,6 +455,76 @@ int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images,
                          const int* w, const int* h, const int* stride,
                          int images_on_device, float scaleFactor, int minObjectSize,
                          int repeats, vj_detect_config* chosen, double* chosenMs);
+
+/* ------------------------------------------------------------------------ */
+/* Serving loop (no reference counterpart; the reference detects one image  */
+/* per call, src/main.cu:2394-2579).                                        */
+/*                                                                          */
+/* Requests of any size are queued as they arrive.  Each worker owns a      */
+/* detector and a CUDA stream; when a worker is free it takes every queued  */
+/* request that fits its share of the HBM budget (by                        */
+/* vj_detect_estimate_bytes) and runs them as one vj_detect_batch launch,   */
+/* so requests arriving while other batches are on the GPU join the next    */
+/* one (continuous batching).  Workers' launches share the GPU: each uses   */
+/* blocksPerSM CTAs per SM (0 = the SM's capacity split evenly among the    */
+/* workers), so two batches run on the device at once.  Every result equals */
+/* vj_detect on that image alone.                                           */
+/* ------------------------------------------------------------------------ */
+
+typedef struct vj_server vj_server;
+
+typedef struct vj_server_config {
+    int32_t winW, winH;            /* model window */
+    int32_t maxImageW, maxImageH;  /* largest request image */
+    int32_t workers;               /* in-flight batches (>= 1) */
+    int32_t maxBatchImages;        /* images per batch at most (1 = plain per-image detect) */
+    int64_t hbmBudgetBytes;        /* device bytes for all in-flight batches */
+    float scaleFactor;             /* detectMultiScale arguments for every request */
+    int32_t minNeighbors;
+    int32_t minObjectSize;
+    int32_t maxDetections;
+    int32_t applyGrouping;
+    int32_t blocksPerSM;           /* persistent CTAs per SM per worker; 0 = split evenly */
+    int32_t tileRows;              /* launch shape (vj_detect_config); 0 = default */
+    int32_t tileStumps;
+} vj_server_config;
+
+typedef struct vj_server_stats {
+    int64_t submitted, completed, failed, batches;
+    double meanBatchImages;
+    double meanMs, p50Ms, p99Ms, p999Ms, maxMs;  /* latency: submit to result ready */
+    double elapsedS;                            /* first submit to last completion */
+    double imagesPerS;                          /* completed / elapsedS */
+    int64_t peakAdmittedBytes;                  /* high-water mark of admitted estimates */
+    int64_t deviceBytes;                        /* work buffers the workers' detectors hold */
+} vj_server_stats;
+
+/* Copies the model (as vj_detector_set_model) and starts the workers. */
+int vj_server_create(const vj_server_config* cfg, const vj_haar_feature* features,
+                     int64_t featureCount, const vj_stump4* stumps, int64_t stumpCount,
+                     const vj_cascade_stage* stages, int64_t stageCount, vj_server** out);
+
+/* Queues a host image (copied; the caller may reuse its buffer at once) and
+ * returns a ticket.  VJ_OUT_OF_MEMORY if the image alone exceeds a worker's
+ * share of the budget. */
+int vj_server_submit(vj_server* s, const uint8_t* image, int w, int h, int stride,
+                     uint64_t* ticket);
+
+/* *done = 1 once the ticket's result is ready. */
+int vj_server_poll(vj_server* s, uint64_t ticket, int* done);
+
+/* Waits up to timeoutMs (< 0: no limit) for the ticket, copies up to
+ * capacity detections to out, sets *count and releases the ticket.  Returns
+ * VJ_RUNTIME_ERROR on timeout (the ticket stays valid) and the batch's status
+ * if its detection failed. */
+int vj_server_wait(vj_server* s, uint64_t ticket, int timeoutMs, vj_detection* out,
+                   int capacity, int* count);
+
+int vj_server_get_stats(vj_server* s, vj_server_stats* out);
+int vj_server_reset_stats(vj_server* s);
+
+/* Finishes the queued requests, stops the workers and frees everything. */
+int vj_server_destroy(vj_server* s);
 
 /* ------------------------------------------------------------------------ */
 /* Synthetic inputs (no reference counterpart: they stand in for the Kaggle  */

@@ -166,3 +166,40 @@ def test_invalid_arguments_fail_loudly(vj):
     assert b"invalid" in vj.load().vj_last_error()
     with pytest.raises(vj.VJError):
         vj.synth_cascade(1, 0, 10)
+
+
+def test_detect_estimate_bytes_grows_with_the_image(vj):
+    sizes = [(320, 240), (640, 480), (1920, 1080), (3840, 2160)]
+    est = [vj.estimate_detect_bytes(w, h) for w, h in sizes]
+    assert all(a < b for a, b in zip(est, est[1:]))
+    # at least the image, its sums (4 B) and squared sums (8 B) per pixel
+    assert est[2] > 1920 * 1080 * 13
+    assert vj.estimate_detect_bytes(20, 20) > 0  # smaller than the window: no level, the image copy only
+
+
+def test_server_config_is_validated(vj, basic_pool):
+    """Bad server configurations are refused before any device work."""
+    st, sg = vj.synth_cascade(2)
+    f, s, g = basic_pool.view(vj.HAAR_FEATURE), st.view(vj.STUMP4), sg.view(vj.STAGE)
+    for bad in (dict(workers=0), dict(maxBatchImages=0), dict(hbmBudgetBytes=0), dict(scaleFactor=1.0),
+                dict(blocksPerSM=-1)):
+        with pytest.raises(vj.VJError) as ei:
+            vj.DetectServer(f, s, g, **bad)
+        assert ei.value.status == vj.Status.kInvalidArg
+
+
+def test_group_rectangles_large_input_matches_oracle(vj, oracle, basic_pool):
+    """Thousands of raw detections from the oracle's detect restatement: the
+    library's grouping (swept from x-sorted arrays with a y prefilter) gives
+    the oracle's clusters in the oracle's order."""
+    st, sg = vj.synth_cascade(2)
+    scene = vj.synth_scene(7, 800, 600, 12, 24, 200)
+    raw = oracle.detect(basic_pool, st, sg, scene, norm_mode=0, threads=8)
+    assert len(raw) > 1000
+    lib = vj.load()
+    for minn in (1, 4, 8):
+        out = np.zeros(len(raw), dtype=vj.DETECTION)
+        n = C.c_int()
+        assert lib.vj_group_rectangles(raw.ctypes.data, len(raw), minn, C.c_float(0.2), out.ctypes.data,
+                                       C.byref(n)) == 0
+        assert out[: n.value].tobytes() == oracle.group(raw, minn, 0.2).tobytes()

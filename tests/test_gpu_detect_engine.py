@@ -17,6 +17,7 @@ CONFIGS = [
     dict(tileRows=8, tileStumps=36, queueStumps=400, blocksPerSM=0),
     dict(tileRows=8, tileStumps=11, queueStumps=2000, blocksPerSM=2),
     dict(tileRows=4, tileStumps=100000, queueStumps=0, blocksPerSM=1),
+    dict(tileRows=16, tileStumps=61, queueStumps=0, blocksPerSM=4),
 ]
 
 
@@ -112,3 +113,22 @@ def test_batch_on_device_images(cuda, vj, basic_pool, full_case):
     assert host_res[0].tobytes() == ref.tobytes()
     for a, b in zip(host_res, dev_res):
         assert a.tobytes() == b.tobytes()
+
+
+def test_reserved_arena(cuda, vj, basic_pool, full_case):
+    """With a reserved arena every batch is laid out inside it: same results,
+    the detector holds no more than the reservation (plus the model and the
+    plan), and a batch that does not fit is refused."""
+    st, sg, scene, ref = full_case
+    e = engine(vj, basic_pool, st, sg)
+    assert e.reserve(512 << 20) == 0
+    h, w = scene.shape
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0 and raw.tobytes() == ref.tobytes()
+    assert (512 << 20) <= e.deviceBytes() < (512 << 20) + (8 << 20)
+    assert e.reserve(1 << 20) == 0
+    s, _ = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == vj.Status.kOutOfMemory
+    assert e.reserve(0) == 0  # back to buffers grown on demand
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0 and raw.tobytes() == ref.tobytes()
