@@ -6,9 +6,15 @@ sort of all 162,336 Basic features (kept resident for the stage), then 50
 boosting rounds, each = best-weak search (bit-exact picks of the reference's
 search) + FP64 AdaBoost update + stage calibration.
 
-metric "stump GB/s": 20 bytes per (feature, sample) per round (f32 key write
+value (stump GB/s): 20 bytes per (feature, sample) per round (f32 key write
 + read, sorted (f32 key, u16 index) pair write + read: one materialisation of
 the sort-based algorithm) x 162,336 x 20,000 x 50 / step time.
+
+The same line carries, under "detect", the detection workloads: plain
+multiscale detect of a 1920x1080 scene, batched detect of 256 scenes of
+uneven sizes, and the serving loop (Poisson arrivals, continuous batching,
+16 GiB HBM budget) against plain per-image detect on the same trace, with
+images/s and p50/p99/p999 latency; plus a CPU baseline of each.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -36,7 +42,9 @@ NPOS = NNEG = 10000
 ROUNDS = 50
 SEED = 1
 BYTES_PER_ELEM_ROUND = 20  # algorithmic model of the stump search
-METRIC = "stump GB/s"
+# BASELINE's metric; `value` is its stump GB/s part (the stage training step),
+# the served images/s and latencies are under "detect".
+METRIC = "served images/s + p50/p99 ms vs plain detect at equal dets; stump GB/s"
 
 
 def peaks():
@@ -267,7 +275,8 @@ def run_gpu(args, rank, world):
     gpu_launches = sum(v[0] for v in prof.values())
 
     result = {
-        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "GB/s", "value_is": "stump GB/s of the stage training step",
+        "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (int32 responses, FP64 renorm)", "data": "synthetic",
         "config": {"workload": "full stage training step (BASELINE configs[1]): 10,000+10,000 24x24 patches "
@@ -288,7 +297,168 @@ def run_gpu(args, rank, world):
         result["cpu_baseline"] = cpu_baseline(pool, patches)
     if dist:
         dist.destroy_process_group()
+        dist = None
+    if rank == 0 and not args.no_detect:
+        det = run_detect(V, torch, quick=args.quick_detect)
+        det["workloads"] = {
+            "plain_1080p": "one 1920x1080 synthetic scene (1/f texture, 40 pasted faces 24-300 px), "
+                           "scaleFactor 1.25, minNeighbors 4, minObjectSize 24, 38-stage / 6,061-stump cascade; "
+                           "host image in, grouped detections out, per call",
+            "batch_256": "256 synthetic scenes, sizes log-uniform 320x240..3840x2160 (425.7 MP), same cascade; "
+                         "pinned host images in, grouped detections out; one persistent launch per batch",
+            "serving": "Poisson arrivals of requests drawn from the same 256 scenes; 16 GiB HBM budget; "
+                       "plain = one image per launch (maxBatchImages 1, one worker)"}
+        result["detect"] = det
     return result
+
+
+# ----------------------------------------------------------------------------- detection and serving
+BATCH_SCENES = 256
+
+
+def detect_inputs(V):
+    """The synthetic detection workloads: the 38-stage / 6,061-stump cascade,
+    one 1920x1080 scene with 40 pasted faces (plain detect), and 256 scenes of
+    log-uniform sizes from 320x240 to 3840x2160 with 5 faces each (batched
+    detect and serving).  Scenes are generated on all host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+    pool = V.feature_pool(V.FeatureMode.Basic)
+    st, sg = V.synth_cascade(2)
+    rng = np.random.default_rng(3)
+    sizes = []
+    for _ in range(BATCH_SCENES):
+        t = rng.random()
+        sizes.append((int(round(320 * 12 ** t)), int(round(240 * 9 ** t))))
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        scenes = list(ex.map(lambda a: V.synth_scene(1000 + a[0], a[1][0], a[1][1], 5, 24, 300), enumerate(sizes)))
+    scene1080 = V.synth_scene(1, 1920, 1080, 40, 24, 300)
+    return pool, st, sg, scene1080, scenes
+
+
+def serve_trace(srv, scenes, rate, n, seed):
+    """Poisson arrivals at `rate` req/s of n requests drawn from `scenes`;
+    returns the server's statistics and the results in request order."""
+    arr = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, n))
+    picks = np.random.default_rng(seed + 1).integers(0, len(scenes), n)
+    tickets = [None] * n
+    res = [None] * n
+
+    def waiter():
+        for i in range(n):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            _, res[i] = srv.wait(tickets[i])
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    srv.resetStats()
+    t0 = time.perf_counter()
+    for i in range(n):
+        dl = t0 + arr[i] - time.perf_counter()
+        if dl > 0:
+            time.sleep(dl)
+        tickets[i] = srv.submit(scenes[picks[i]])
+    th.join()
+    return srv.stats(), res, picks
+
+
+def run_detect(V, torch, quick=False):
+    pool, st, sg, scene1080, scenes = detect_inputs(V)
+    f, s, g = pool.view(V.HAAR_FEATURE), st.view(V.STUMP4), sg.view(V.STAGE)
+    e = V.FaceVisionEngine((24, 24), 1, 3840, 2160, False, 200000)
+    assert e.setCascadeModel(f, s, g) == 0
+    out = {}
+    # ---- plain multiscale detect of one 1920x1080 image (host image in, grouped detections out)
+    for _ in range(3):
+        e.detectMultiScale(scene1080, 1920, 1080, 1920)
+    reps = 10
+    t = time.perf_counter()
+    for _ in range(reps):
+        st_, grp = e.detectMultiScale(scene1080, 1920, 1080, 1920)
+    ms = (time.perf_counter() - t) / reps * 1e3
+    k = e.lastStats()
+    out["plain_1080p"] = {"images_per_s": 1e3 / ms, "ms_per_image": ms, "gpu_ms": k["gpuMs"],
+                          "host_ms": k["hostMs"], "phase_ms": k["phaseMs"], "raw_detections": k["rawDetections"],
+                          "grouped_detections": int(len(grp)), "windows": k["windows"],
+                          "stump_evals": k["stumpEvals"], "stumps_per_s_gpu": k["stumpEvals"] / (k["gpuMs"] * 1e-3)}
+    # ---- batched detect of 256 scenes
+    s_, cfg, tune_ms = e.autotune(scenes[:32], repeats=1)
+    pinned = []
+    for sc in scenes:
+        tp = torch.from_numpy(sc).pin_memory()
+        pinned.append(tp.numpy())
+    e.detectBatch(pinned, capPerImage=4096)
+    times = []
+    for _ in range(2 if quick else 3):
+        t = time.perf_counter()
+        s_, batch = e.detectBatch(pinned, capPerImage=4096)
+        times.append(time.perf_counter() - t)
+    kb = e.lastStats()
+    bt = statistics.median(times)
+    dev = [torch.from_numpy(sc).cuda() for sc in scenes]
+    e.detectBatch(dev, capPerImage=4096)
+    t = time.perf_counter()
+    e.detectBatch(dev, capPerImage=4096)
+    bt_dev = time.perf_counter() - t
+    del dev
+    # plain per-image detect over the same scenes, and the identity check
+    t = time.perf_counter()
+    same = True
+    for i, sc in enumerate(pinned):
+        s_, one = e.detectMultiScale(sc, sc.shape[1], sc.shape[0], sc.shape[1])
+        same = same and one.tobytes() == batch[i].tobytes()
+    pt = time.perf_counter() - t
+    px = sum(sc.size for sc in scenes)
+    out["batch_256"] = {"images_per_s": len(scenes) / bt, "s_per_batch": bt, "gpu_ms": kb["gpuMs"],
+                        "host_ms": kb["hostMs"], "phase_ms": kb["phaseMs"],
+                        "images_per_s_device_images": len(scenes) / bt_dev,
+                        "megapixels": px / 1e6, "pyramid_pixels": kb["pyramidPixels"], "windows": kb["windows"],
+                        "stump_evals": kb["stumpEvals"], "stumps_per_s_gpu": kb["stumpEvals"] / (kb["gpuMs"] * 1e-3),
+                        "raw_detections": kb["rawDetections"], "autotuned_config": cfg, "autotune_best_ms_32": tune_ms,
+                        "plain_images_per_s_same_scenes": len(scenes) / pt,
+                        "batch_over_plain": pt / bt, "identical_to_plain_per_image": bool(same)}
+    e = None
+    # ---- serving: Poisson arrivals of the same scenes, continuous batching vs plain per-image detect
+    serving = {}
+    rates = [200] if quick else [200, 1000, 2000]
+    plain_res = None
+    srv = V.DetectServer(f, s, g, workers=1, maxBatchImages=1, hbmBudgetBytes=16 << 30)
+    serve_trace(srv, scenes, 200, 32, 99)
+    n_plain = 400 if quick else 1000
+    k, plain_res, picks = serve_trace(srv, scenes, 200, n_plain, 7)
+    srv.close()
+    serving["plain_per_image"] = {"rate_req_s": 200, "requests": n_plain, "images_per_s": k["imagesPerS"],
+                                  "p50_ms": k["p50Ms"], "p99_ms": k["p99Ms"], "p999_ms": k["p999Ms"],
+                                  "mean_batch_images": k["meanBatchImages"]}
+    srv = V.DetectServer(f, s, g, workers=3, maxBatchImages=256, hbmBudgetBytes=16 << 30,
+                         tileRows=cfg["tileRows"], tileStumps=cfg["tileStumps"])
+    serve_trace(srv, scenes, 200, 64, 99)
+    for rate in rates:
+        n = n_plain if rate == 200 else (1000 if quick else 2000)
+        k, res, _ = serve_trace(srv, scenes, rate, n, 7)
+        ent = {"rate_req_s": rate, "requests": n, "images_per_s": k["imagesPerS"], "p50_ms": k["p50Ms"],
+               "p99_ms": k["p99Ms"], "p999_ms": k["p999Ms"], "mean_batch_images": k["meanBatchImages"],
+               "peak_admitted_gb": k["peakAdmittedBytes"] / 1e9, "device_gb": k["deviceBytes"] / 1e9}
+        if rate == 200:
+            ent["identical_to_plain"] = all(a.tobytes() == b.tobytes() for a, b in zip(res, plain_res))
+        serving[f"batched_{rate}"] = ent
+    srv.close()
+    serving["hbm_budget_gb"] = (16 << 30) / 1e9
+    serving["workers"] = 3
+    best = max(v["images_per_s"] for kk, v in serving.items() if kk.startswith("batched_"))
+    serving["batched_over_plain_images_per_s"] = best / serving["plain_per_image"]["images_per_s"]
+    out["serving"] = serving
+    # ---- CPU baseline: the oracle's restatement of detectMultiScaleCpu on all host threads
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    thr = os.cpu_count() or 1
+    t = time.perf_counter()
+    O.detect(pool, st, sg, scene1080, norm_mode=0, threads=thr)
+    cdt = time.perf_counter() - t
+    out["cpu_baseline"] = {"value": 1.0 / cdt, "unit": "images/s", "cores": thr, "kind": "port",
+                           "sample": "one 1920x1080 scene through the oracle's restatement of detectMultiScaleCpu "
+                                     f"(raw detections, no grouping), {cdt:.2f} s"}
+    return out
 
 
 # ----------------------------------------------------------------------------- CPU (oracle) arm
@@ -331,7 +501,17 @@ def run_reference(args, rank, world):
     times = [cpu_sample(pool, patches, nfeat, threads) for _ in range(args.steps)]
     dt = sum(times) / len(times)
     value = BYTES_PER_ELEM_ROUND * nfeat * n / dt / 1e9
+    # detection: the oracle's restatement of detectMultiScaleCpu on one 1920x1080 scene
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    st, sg = V.synth_cascade(2)
+    scene = V.synth_scene(1, 1920, 1080, 40, 24, 300)
+    t = time.perf_counter()
+    raw = O.detect(pool, st, sg, scene, norm_mode=0, threads=threads)
+    cdt = time.perf_counter() - t
     return {
+        "detect": {"plain_1080p": {"images_per_s": 1.0 / cdt, "ms_per_image": cdt * 1e3, "cores": threads,
+                                   "raw_detections": int(len(raw))}},
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -354,6 +534,8 @@ def main():
     ap.add_argument("--features", type=int, default=162336, help="first K Basic features (profiling cases)")
     ap.add_argument("--rounds", type=int, default=50, help="boosting rounds per step (profiling cases)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-detect", action="store_true", help="stump step only")
+    ap.add_argument("--quick-detect", action="store_true", help="shorter serving traces")
     args = ap.parse_args()
     global ROUNDS
     ROUNDS = args.rounds
