@@ -461,6 +461,44 @@ def run_detect(V, torch, quick=False):
     return out
 
 
+def run_detect_case(args):
+    """One detection case alone (profiling runs): `plain1080` (the 1920x1080
+    scene) or `batchN` (the first N of the 256 scenes in one batch); W warm-up
+    and K timed calls, then one JSON line with the work counters."""
+    import torch
+
+    import cs677s26_gb300 as V
+    case = args.detect_case
+    pool = V.feature_pool(V.FeatureMode.Basic)
+    st, sg = V.synth_cascade(2)
+    e = V.FaceVisionEngine((24, 24), 1, 3840, 2160, False, 200000)
+    assert e.setCascadeModel(pool, st, sg) == 0
+    if args.detect_config:
+        assert e.setConfig(**json.loads(args.detect_config)) == 0
+    if case == "plain1080":
+        scene = V.synth_scene(1, 1920, 1080, 40, 24, 300)
+        call = lambda: e.detectMultiScale(scene, 1920, 1080, 1920)  # noqa: E731
+    elif case.startswith("batch"):
+        k = int(case[5:])
+        rng = np.random.default_rng(3)
+        scenes = []
+        for i in range(k):
+            t = rng.random()
+            scenes.append(V.synth_scene(1000 + i, int(round(320 * 12 ** t)), int(round(240 * 9 ** t)), 5, 24, 300))
+        call = lambda: e.detectBatch(scenes, capPerImage=4096)  # noqa: E731
+    else:
+        raise SystemExit(f"unknown detect case {case}")
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        status, _ = call()
+    dt = (time.perf_counter() - t) / max(1, args.steps)
+    return {"detect_case": case, "config": e.getConfig(), "status": int(status), "ms_per_call": dt * 1e3,
+            "stats": e.lastStats()}
+
+
 # ----------------------------------------------------------------------------- CPU (oracle) arm
 def cpu_sample(pool, patches, nfeat, threads):
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -536,12 +574,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-detect", action="store_true", help="stump step only")
     ap.add_argument("--quick-detect", action="store_true", help="shorter serving traces")
+    ap.add_argument("--detect-case", default=None, help="run one detection case alone: plain1080 or batchN")
+    ap.add_argument("--detect-config", default=None, help="launch shape for --detect-case, as JSON")
     args = ap.parse_args()
     global ROUNDS
     ROUNDS = args.rounds
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    if args.impl == "reference":
+    if args.detect_case:
+        res = run_detect_case(args)
+    elif args.impl == "reference":
         res = run_reference(args, rank, world)
     else:
         res = run_gpu(args, rank, world)

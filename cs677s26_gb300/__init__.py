@@ -233,7 +233,7 @@ class FaceVisionEngine:
     def getConfig(self) -> dict:
         rec = np.zeros(1, dtype=_capi.DETECT_CONFIG)
         call("vj_detector_get_config", self._h, ptr(rec))
-        return {k: int(rec[k][0]) for k in _capi.DETECT_CONFIG.names}
+        return {k: int(rec[k][0]) for k in _capi.DETECT_CONFIG.names if k != "reserved"}
 
     def setConfig(self, **cfg) -> int:
         """Launch shape of the detection kernel (tileRows, tileStumps, queueStumps, blocksPerSM)."""
@@ -255,7 +255,7 @@ class FaceVisionEngine:
         ms = C.c_double()
         st = _capi.status("vj_detector_autotune", self._h, n, ptrs, ws, hs, ws, int(on_dev), C.c_float(scaleFactor),
                           minObjectSize, repeats, ptr(rec), C.byref(ms))
-        return Status(st), {k: int(rec[k][0]) for k in _capi.DETECT_CONFIG.names}, ms.value
+        return Status(st), {k: int(rec[k][0]) for k in _capi.DETECT_CONFIG.names if k != "reserved"}, ms.value
 
 
 def estimate_detect_bytes(w: int, h: int, scaleFactor: float = 1.25, minObjectSize: int = 24,

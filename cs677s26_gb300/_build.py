@@ -80,7 +80,35 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         if r.returncode != 0:
             raise RuntimeError("libvjgb link failed:\n" + r.stdout.decode(errors="replace"))
+    build_tools(verbose, force)
     return LIB
+
+
+TOOLS = CSRC / "tools"
+BIN = PKG / "bin"
+
+
+def build_tools(verbose: bool = False, force: bool = False) -> list[Path]:
+    """Command-line drop-ins (vj_detect ...) linked against libvjgb.so."""
+    BIN.mkdir(exist_ok=True)
+    cuda_lib = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "lib64"
+    out = []
+    procs = []
+    for src in sorted(TOOLS.glob("*.cpp")):
+        exe = BIN / src.stem
+        out.append(exe)
+        if not force and exe.exists() and exe.stat().st_mtime > max(src.stat().st_mtime, LIB.stat().st_mtime):
+            continue
+        cmd = [CXX, *CXXFLAGS, "-I", str(INCLUDE), "-I", "/usr/local/cuda/include", str(src), "-o", str(exe),
+               "-L", str(PKG), "-lvjgb", "-L", str(cuda_lib), "-lcudart", "-Wl,-rpath,$ORIGIN/..", "-lpthread"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    for src, p in procs:
+        text, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f"{src.name} build failed:\n" + text.decode(errors="replace"))
+    return out
 
 
 if __name__ == "__main__":

@@ -40,7 +40,8 @@ DETECT_STATS = np.dtype([("images", "<i8"), ("levels", "<i8"), ("pyramidPixels",
                          ("gated", "<i8"), ("stumpEvals", "<i8"), ("rawDetections", "<i8"), ("deepWindows", "<i8"),
                          ("attempts", "<i4"), ("queuePasses", "<i4"), ("gpuMs", "<f8"), ("phaseMs", "<f8", 6),
                          ("hostMs", "<f8", 3)])
-DETECT_CONFIG = np.dtype([("tileRows", "<i4"), ("tileStumps", "<i4"), ("queueStumps", "<i4"), ("blocksPerSM", "<i4")])
+DETECT_CONFIG = np.dtype([("tileRows", "<i4"), ("tileStumps", "<i4"), ("queueStumps", "<i4"), ("blocksPerSM", "<i4"),
+                          ("deepSlots", "<i4"), ("reserved", "<i4")])
 SERVER_CONFIG = np.dtype([("winW", "<i4"), ("winH", "<i4"), ("maxImageW", "<i4"), ("maxImageH", "<i4"),
                           ("workers", "<i4"), ("maxBatchImages", "<i4"), ("hbmBudgetBytes", "<i8"),
                           ("scaleFactor", "<f4"), ("minNeighbors", "<i4"), ("minObjectSize", "<i4"),
@@ -53,7 +54,7 @@ SERVER_STATS = np.dtype([("submitted", "<i8"), ("completed", "<i8"), ("failed", 
 PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "compaction")
 HOST_PHASES = ("plan_upload", "wait", "sort_group")
 
-assert DETECT_STATS.itemsize == 152 and DETECT_CONFIG.itemsize == 16
+assert DETECT_STATS.itemsize == 152 and DETECT_CONFIG.itemsize == 24
 assert SERVER_CONFIG.itemsize == 64 and SERVER_STATS.itemsize == 112
 assert HAAR_FEATURE.itemsize == 64 and STUMP4.itemsize == 16 and STAGE.itemsize == 12
 assert DETECTION.itemsize == 24 and TILE_BEST.itemsize == 16 and WEAK.itemsize == 28

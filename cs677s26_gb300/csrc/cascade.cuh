@@ -496,63 +496,107 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
 }
 
 // ---------------------------------------------------------------------------
-// Warp-per-window deep pass.  A warp takes one window at a time, copies its
-// (winW+1) x (winH+1) integral patch into shared memory as floats, and runs
-// the remaining stages with lane k evaluating stump k of each group of 32; the
-// stage sum then adds the 32 leaf values in stump order (shuffles from lane
-// 0, 1, ...), so it is the same sequential fp32 sum as the reference's.
+// Deep pass: SL windows per warp, 32/SL lanes per window.  Each window slot
+// holds the window's (winW+1) x (winH+1) integral patch in shared memory as
+// floats; per step every slot evaluates its next 32/SL stumps (lane j of the
+// slot: stump k0 + j), the values go through a per-warp shared buffer, and
+// each slot adds its values to its stage sum in stump order, so the sum is
+// the same sequential fp32 sum as the reference's.  A slot whose window is
+// rejected or accepted takes the next window from the queue; the whole warp
+// copies the new window's patch.
+//
+// Per-warp shared memory: 32 floats of values, then SL patches.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void deep_pass(const DevPlan& P, float* patch, const QEntry* q, int n,
+__host__ __device__ constexpr int deep_warp_floats(int slots, int patchElems) {
+    return 32 + ((slots * patchElems + 3) & ~3);
+}
+
+template <int SL>
+__device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QEntry* q, int n,
                                           unsigned long long* workCounter, unsigned long long& evals) {
+    constexpr int LPS = 32 / SL;  // lanes per slot
     const int lane = threadIdx.x & 31;
-    const int pw = P.winW + 1, ph = P.winH + 1;
-    const int warps = gridDim.x * kCasWarps;
-    const int take = max(1, min(16, n / (warps * 8)));
+    const int slot = lane / LPS, j = lane % LPS;
+    const int pw = P.winW + 1, ph = P.winH + 1, pe = pw * ph;
+    float* vals = wsm;
+    float* patches = wsm + 32;
+    const float* myPatch = patches + slot * pe;
+    int qi = -1;  // queue index of the slot's window, -1 = empty
+    QEntry e{};
+    int si = 0, k0 = 0;
+    float acc = 0.0f, score = 0.0f;
+    bool more = true;
     for (;;) {
-        unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(workCounter, static_cast<unsigned long long>(take));
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= static_cast<unsigned long long>(n)) break;
-        const int end = static_cast<int>(min(static_cast<unsigned long long>(n), t + take));
-        for (int i = static_cast<int>(t); i < end; ++i) {
-            const QEntry e = q[i];
-            const CasLevel& L = P.levels[e.level];
+        // Refill empty slots one window at a time; all lanes copy the patch.
+        while (more) {
+            const unsigned empty = __ballot_sync(0xffffffffu, qi < 0 && j == 0);
+            if (!empty) break;
+            const int s = (__ffs(empty) - 1) / LPS;
+            unsigned long long t = 0;
+            if (lane == 0) t = atomicAdd(workCounter, 1ull);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            if (t >= static_cast<unsigned long long>(n)) {
+                more = false;
+                break;
+            }
+            const QEntry ne = q[t];
+            const CasLevel& L = P.levels[ne.level];
             const uint32_t* sum = L.sum;
             const int64_t Pi = L.pitch;
-            const int64_t b = static_cast<int64_t>(e.xy >> 16) * Pi + static_cast<int64_t>(e.xy & 0xFFFFu);
-            __syncwarp();
+            const int64_t b = static_cast<int64_t>(ne.xy >> 16) * Pi + static_cast<int64_t>(ne.xy & 0xFFFFu);
+            float* dst = patches + s * pe;
             for (int r = 0; r < ph; ++r)
-                for (int c = lane; c < pw; c += 32) patch[r * pw + c] = corner_f(sum[b + r * Pi + c]);
-            __syncwarp();
-            float score = e.score;
-            bool alive = true;
-            for (int si = P.deepFrom; si < P.nStages; ++si) {
-                const DStage st = P.stages[si];
-                float acc = 0.0f;
-                for (int k0 = 0; k0 < st.ntrees; k0 += 32) {
-                    const int k = k0 + lane;
-                    float c = 0.0f;
-                    if (k < st.ntrees) c = patch_stump_value(P.pstumps, st.first + k, patch, e.inv);
-                    const int m = min(32, st.ntrees - k0);
-                    if (m == 32) {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, c, j));
-                    } else {
-                        for (int j = 0; j < m; ++j) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, c, j));
-                    }
-                }
-                evals += static_cast<unsigned>(st.ntrees);
-                if (acc < st.threshold) {
-                    alive = false;
-                    break;
-                }
-                score = acc;
+                for (int c = lane; c < pw; c += 32) dst[r * pw + c] = corner_f(sum[b + r * Pi + c]);
+            if (slot == s) {
+                qi = static_cast<int>(t);
+                e = ne;
+                si = P.deepFrom;
+                k0 = 0;
+                acc = 0.0f;
+                score = ne.score;
             }
-            if (alive && lane == 0) {
-                const int image = L.image;
-                const int slot = atomicAdd(P.counts + image, 1);
-                if (slot < P.detCap)
-                    P.dets[static_cast<size_t>(image) * P.detCap + slot] = make_detection(L, e, P.winW, P.winH, score);
+        }
+        if (!__any_sync(0xffffffffu, qi >= 0)) break;
+        __syncwarp();
+        const bool active = qi >= 0;
+        DStage st{0, 0, 0.0f, 0};
+        if (active) st = P.stages[si];
+        const int k = k0 + j;
+        float c = 0.0f;
+        if (active && k < st.ntrees) c = patch_stump_value(P.pstumps, st.first + k, myPatch, e.inv);
+        vals[lane] = c;
+        __syncwarp();
+        const int m = active ? min(LPS, st.ntrees - k0) : 0;
+        const float4* v4 = reinterpret_cast<const float4*>(vals + slot * LPS);
+#pragma unroll
+        for (int g = 0; g < LPS / 4; ++g) {
+            const float4 x = v4[g];
+            if (4 * g + 0 < m) acc = __fadd_rn(acc, x.x);
+            if (4 * g + 1 < m) acc = __fadd_rn(acc, x.y);
+            if (4 * g + 2 < m) acc = __fadd_rn(acc, x.z);
+            if (4 * g + 3 < m) acc = __fadd_rn(acc, x.w);
+        }
+        __syncwarp();
+        if (j == 0) evals += static_cast<unsigned>(m);
+        k0 += LPS;
+        if (active && k0 >= st.ntrees) {
+            if (acc < st.threshold) {
+                qi = -1;
+            } else {
+                score = acc;
+                ++si;
+                k0 = 0;
+                acc = 0.0f;
+                if (si >= P.nStages) {
+                    if (j == 0) {
+                        const CasLevel& L = P.levels[e.level];
+                        const int slotOut = atomicAdd(P.counts + L.image, 1);
+                        if (slotOut < P.detCap)
+                            P.dets[static_cast<size_t>(L.image) * P.detCap + slotOut] =
+                                make_detection(L, e, P.winW, P.winH, score);
+                    }
+                    qi = -1;
+                }
             }
         }
     }
@@ -569,7 +613,7 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* patch, const 
 //   6. compaction of the raw detections, image after image, into the
 //      host-mapped buffer.
 // ---------------------------------------------------------------------------
-template <int TH, int MINB>
+template <int TH, int MINB, int SL>
 __global__ void __launch_bounds__(kCasThreads, MINB)
 detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     extern __shared__ __align__(16) unsigned char dsmem[];
@@ -604,7 +648,7 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     if (!grid_barrier(G, epoch)) return;
     if (stamper) G->stamp[2] = global_ns();
 
-    unsigned long long gated = 0, evals = 0;
+    unsigned long long gated = 0, evals = 0, deepEvals = 0;
     QEntry* lst = reinterpret_cast<QEntry*>(dsmem) + static_cast<size_t>(wib) * 32 * TH;
 
     // 3. tile pass -> queue 0 (or detections)
@@ -626,12 +670,18 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     if (P.deepFrom < P.nStages) {
         const int m = P.nQueuePasses;
         const int nIn = min(C->qcount[m], P.qcap);
-        float* patch = reinterpret_cast<float*>(dsmem) + static_cast<size_t>(wib) * (P.winW + 1) * (P.winH + 1);
-        deep_pass(P, patch, P.q[m & 1], nIn, &C->work[kQueues], evals);
+        float* wsm = reinterpret_cast<float*>(dsmem) +
+                     static_cast<size_t>(wib) * deep_warp_floats(SL, (P.winW + 1) * (P.winH + 1));
+        deep_pass<SL>(P, wsm, P.q[m & 1], nIn, &C->work[kQueues], deepEvals);
     }
+    // lane passes count the same totals in every lane; the deep pass counts
+    // per slot in the slot's first lane
+    unsigned long long deepSum = deepEvals;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) deepSum += __shfl_xor_sync(0xffffffffu, deepSum, o);
     if (lane == 0) {
         if (gated) atomicAdd(&C->stats[0], gated);
-        if (evals) atomicAdd(&C->stats[1], evals);
+        if (evals + deepSum) atomicAdd(&C->stats[1], evals + deepSum);
     }
     if (!grid_barrier(G, epoch)) return;
     if (stamper) G->stamp[5] = global_ns();

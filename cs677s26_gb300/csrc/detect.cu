@@ -179,7 +179,7 @@ struct vj_detector {
     // range of it, so the detector never holds more than its reservation.
     DBuf arena;
     // Launch shape and the stage schedule derived from it.
-    vj_detect_config cfg{8, 64, 0, 0};
+    vj_detect_config cfg{8, 64, 0, 4, 2, 0};
     int tileStages = 0, deepFrom = 0;
     std::vector<int> queueEnds;
     // Launch graph and what it was built for.
@@ -187,6 +187,7 @@ struct vj_detector {
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t planNode = nullptr;
     int graphTH = 0, graphGrid = 0;
+    const void* graphFn = nullptr;
     size_t graphSmem = 0, graphCtrlBytes = 0;
     void* graphPlan = nullptr;
     void* graphCtrl = nullptr;
@@ -236,28 +237,33 @@ void schedule_passes(vj_detector* d) {
     d->deepFrom = d->queueEnds.empty() ? d->tileStages : d->queueEnds.back();
 }
 
-template <int TH>
+template <int TH, int SL>
 const void* kernel_for(int blocksPerSM) {
-    if (blocksPerSM >= 4) return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 4>);
-    if (blocksPerSM == 1 || blocksPerSM == 2) return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 2>);
-    return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 3>);
+    if (blocksPerSM >= 4) return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 4, SL>);
+    return reinterpret_cast<const void*>(&detect_persistent_kernel<TH, 3, SL>);
 }
 
-// Kernel variant for a launch shape: tile rows, and the residency the kernel
-// is compiled for - 2, 3 (also for blocksPerSM 0) or 4 CTAs of 256 threads
-// per SM, which caps its registers at 128, 85 or 64.
-const void* kernel_ptr(int th, int blocksPerSM) {
-    switch (th) {
-        case 4: return kernel_for<4>(blocksPerSM);
-        case 16: return kernel_for<16>(blocksPerSM);
-        default: return kernel_for<8>(blocksPerSM);
+template <int TH>
+const void* kernel_for_slots(int blocksPerSM, int slots) {
+    return slots == 4 ? kernel_for<TH, 4>(blocksPerSM) : kernel_for<TH, 2>(blocksPerSM);
+}
+
+// Kernel variant for a launch shape: tile rows, deep-pass window slots, and
+// the residency the kernel is compiled for - 3 (blocksPerSM 0-3) or 4 CTAs of
+// 256 threads per SM, which caps its registers at 85 or 64.
+const void* kernel_ptr(const vj_detect_config& c) {
+    switch (c.tileRows) {
+        case 4: return kernel_for_slots<4>(c.blocksPerSM, c.deepSlots);
+        case 16: return kernel_for_slots<16>(c.blocksPerSM, c.deepSlots);
+        default: return kernel_for_slots<8>(c.blocksPerSM, c.deepSlots);
     }
 }
 
 size_t smem_bytes(const vj_detector* d, int th) {
     const size_t lists = static_cast<size_t>(kCasWarps) * 32 * th * sizeof(QEntry);
-    const size_t patches = static_cast<size_t>(kCasWarps) * (d->winW + 1) * (d->winH + 1) * sizeof(float);
-    return std::max(lists, patches);
+    const size_t deep = static_cast<size_t>(kCasWarps) *
+                        deep_warp_floats(d->cfg.deepSlots, (d->winW + 1) * (d->winH + 1)) * sizeof(float);
+    return std::max(lists, deep);
 }
 
 size_t ctrl_bytes(int imageCap) {
@@ -270,14 +276,14 @@ int ensure_graph(vj_detector* d, size_t planBytes) {
     const int th = d->cfg.tileRows;
     const size_t smem = smem_bytes(d, th);
     const size_t cbytes = ctrl_bytes(d->imageCap);
-    const void* fn = kernel_ptr(th, d->cfg.blocksPerSM);
+    const void* fn = kernel_ptr(d->cfg);
     VJ_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int fit = 0;
     VJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, kCasThreads, smem));
     if (fit < 1) return set_error(VJ_RUNTIME_ERROR, "detection kernel does not fit on an SM");
     const int bps = d->cfg.blocksPerSM > 0 ? std::min(d->cfg.blocksPerSM, fit) : fit;
     const int grid = bps * sm_count();
-    if (d->exec && d->graphTH == th && d->graphGrid == grid && d->graphSmem == smem && d->graphPlan == d->dplan.p &&
+    if (d->exec && d->graphFn == fn && d->graphTH == th && d->graphGrid == grid && d->graphSmem == smem && d->graphPlan == d->dplan.p &&
         d->graphCtrl == d->dctrl.p && d->graphCtrlBytes == cbytes && d->graphHCtrl == d->hctrl.p)
         return VJ_OK;
     drop_graph(d);
@@ -324,6 +330,7 @@ int ensure_graph(vj_detector* d, size_t planBytes) {
     d->exec = x;
     d->planNode = nPlan;
     d->graphTH = th;
+    d->graphFn = fn;
     d->graphGrid = grid;
     d->graphSmem = smem;
     d->graphCtrlBytes = cbytes;
@@ -680,8 +687,9 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
 
 int check_config(const vj_detect_config& c) {
     if ((c.tileRows != 4 && c.tileRows != 8 && c.tileRows != 16) || c.tileStumps < 0 || c.queueStumps < 0 ||
-        c.blocksPerSM < 0)
-        return set_error(VJ_INVALID_ARG, "detection config: tileRows must be 4, 8 or 16 and the rest >= 0");
+        c.blocksPerSM < 0 || (c.deepSlots != 2 && c.deepSlots != 4) || c.reserved != 0)
+        return set_error(VJ_INVALID_ARG,
+                         "detection config: tileRows must be 4, 8 or 16, deepSlots 2 or 4, the rest >= 0");
     return VJ_OK;
 }
 
@@ -852,7 +860,7 @@ int vj_detector_occupancy(vj_detector* d, int* blocksPerSM) {
     if (!d || !blocksPerSM) return set_error(VJ_INVALID_ARG, "vj_detector_occupancy: null argument");
     const int th = d->cfg.tileRows;
     const size_t smem = smem_bytes(d, th);
-    const void* fn = kernel_ptr(th, d->cfg.blocksPerSM);
+    const void* fn = kernel_ptr(d->cfg);
     VJ_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int fit = 0;
     VJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, kCasThreads, smem));
@@ -1004,14 +1012,16 @@ int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images, co
         return VJ_OK;
     };
     for (int th : {8, 4, 16})
-        for (int bps : {0, 4, 2}) {
-            if (st != VJ_OK) break;
-            vj_detect_config c = saved;
-            c.tileRows = th;
-            c.blocksPerSM = bps;
-            c.queueStumps = 0;
-            st = trial(c);
-        }
+        for (int bps : {4, 0})
+            for (int slots : {2, 4}) {
+                if (st != VJ_OK) break;
+                vj_detect_config c = saved;
+                c.tileRows = th;
+                c.blocksPerSM = bps;
+                c.deepSlots = slots;
+                c.queueStumps = 0;
+                st = trial(c);
+            }
     const vj_detect_config shape = bestCfg;
     for (int dep : depths) {
         if (st != VJ_OK) break;

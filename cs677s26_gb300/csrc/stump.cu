@@ -22,8 +22,10 @@
 //   3. Candidates: every feature whose error is within 2*(bound of the
 //      reference's sequential FP32 arithmetic + bound of step 2) of the
 //      minimum.  The reference's pick is provably among them.
-//   4. refine_kernel: one thread per candidate replays the reference's
-//      sequential FP32 totals and sweep exactly (main.cu:626-678); the
+//   4. refine_kernel: one warp per candidate replays the reference's
+//      sequential FP32 totals and sweep exactly (main.cu:626-678): the warp
+//      stages each 256-position chunk's weights in sorted order, one lane
+//      runs the sequential FP32 chain, all lanes score the valid splits; the
 //      winner is the smallest FP32 error, ties to the lower featureIdx.
 // With vj_trainer_prepare_stage the orders of step 1 stay resident in HBM for
 // all rounds of a stage (the responses do not change within a stage, only

@@ -1,0 +1,222 @@
+// vj_detect: the drop-in for `cuda_hello detect` (src/main.cu:2394-2579).
+//
+//   vj_detect <in_model.bin> <image.pgm> <out.ppm>
+//             [scaleFactor=1.25] [minNeighbors=4] [minObjectSize=24]
+//             [maxDetections=200000] [benchmarkRuns=0]
+//
+// Same arguments, defaults and clamps, same console lines, same output image:
+// the grey input as RGB with a 2-pixel white frame around every grouped
+// detection, written as binary PPM.  Detection runs through the library's
+// C ABI (vj_detect with grouping), i.e. the GB300 kernels.
+#include <algorithm>
+#include <cctype>
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "vjgb.h"
+
+namespace {
+
+struct Gray {
+    int w = 0, h = 0;
+    std::vector<uint8_t> px;
+};
+
+// Next header token, skipping whitespace and '#' comment lines.
+bool next_token(std::istream& is, std::string& tok) {
+    tok.clear();
+    while (is.good()) {
+        const int c = is.peek();
+        if (c == '#') {
+            std::string line;
+            std::getline(is, line);
+            continue;
+        }
+        if (c != EOF && std::isspace(static_cast<unsigned char>(c))) {
+            is.get();
+            continue;
+        }
+        break;
+    }
+    if (!is.good()) return false;
+    is >> tok;
+    return !tok.empty();
+}
+
+// Binary P5 PGM with maxval <= 255.
+bool load_pgm(const std::string& path, Gray& g) {
+    std::ifstream ifs(path, std::ios::binary);
+    if (!ifs) {
+        std::cerr << "[ERR] Cannot open PGM: " << path << "\n";
+        return false;
+    }
+    std::string tok;
+    if (!next_token(ifs, tok) || tok != "P5") {
+        std::cerr << "[ERR] Unsupported PGM format (need P5): " << path << "\n";
+        return false;
+    }
+    int maxVal = 0;
+    try {
+        if (!next_token(ifs, tok)) return false;
+        g.w = std::stoi(tok);
+        if (!next_token(ifs, tok)) return false;
+        g.h = std::stoi(tok);
+        if (!next_token(ifs, tok)) return false;
+        maxVal = std::stoi(tok);
+    } catch (...) {
+        std::cerr << "[ERR] Invalid PGM metadata\n";
+        return false;
+    }
+    if (g.w <= 0 || g.h <= 0 || maxVal <= 0 || maxVal > 255) {
+        std::cerr << "[ERR] Invalid PGM metadata\n";
+        return false;
+    }
+    ifs.get();  // the single whitespace after the header
+    g.px.resize(static_cast<size_t>(g.w) * g.h);
+    if (!ifs.read(reinterpret_cast<char*>(g.px.data()), static_cast<std::streamsize>(g.px.size()))) {
+        std::cerr << "[ERR] Failed to read PGM pixel payload\n";
+        return false;
+    }
+    return true;
+}
+
+bool save_ppm(const std::string& path, int w, int h, const std::vector<uint8_t>& rgb) {
+    std::ofstream ofs(path, std::ios::binary);
+    if (!ofs) {
+        std::cerr << "[ERR] Cannot write PPM: " << path << "\n";
+        return false;
+    }
+    ofs << "P6\n" << w << " " << h << "\n255\n";
+    ofs.write(reinterpret_cast<const char*>(rgb.data()), static_cast<std::streamsize>(rgb.size()));
+    return static_cast<bool>(ofs);
+}
+
+// 2-pixel white frame, clipped to the image.
+void draw_frame(std::vector<uint8_t>& rgb, int w, int h, const vj_detection& d) {
+    const int x0 = std::max(0, d.x), y0 = std::max(0, d.y);
+    const int x1 = std::min(w - 1, d.x + d.w - 1), y1 = std::min(h - 1, d.y + d.h - 1);
+    if (x0 > x1 || y0 > y1) return;
+    auto set = [&](int x, int y) {
+        const size_t i = (static_cast<size_t>(y) * w + x) * 3;
+        rgb[i] = rgb[i + 1] = rgb[i + 2] = 255;
+    };
+    for (int t = 0; t < 2; ++t) {
+        const int yt = std::min(h - 1, y0 + t), yb = std::max(0, y1 - t);
+        for (int x = x0; x <= x1; ++x) {
+            set(x, yt);
+            set(x, yb);
+        }
+        const int xl = std::min(w - 1, x0 + t), xr = std::max(0, x1 - t);
+        for (int y = y0; y <= y1; ++y) {
+            set(xl, y);
+            set(xr, y);
+        }
+    }
+}
+
+int fail(const char* what) {
+    std::cerr << "[ERR] " << what << " failed: " << vj_last_error() << "\n";
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 4) {
+        std::cerr << "Usage: vj_detect <in_model.bin> <image.pgm> <out.ppm>"
+                  << " [scaleFactor=1.25] [minNeighbors=4] [minObjectSize=24] [maxDetections=200000] "
+                     "[benchmarkRuns=0]\n";
+        return 1;
+    }
+    const std::string modelPath = argv[1], imagePath = argv[2], outPath = argv[3];
+    float scaleFactor = 1.25f;
+    int minNeighbors = 4, minObjectSize = 24, maxDetections = 200000, benchmarkRuns = 0;
+    try {
+        if (argc > 4) scaleFactor = std::stof(argv[4]);
+        if (argc > 5) minNeighbors = std::max(1, std::stoi(argv[5]));
+        if (argc > 6) minObjectSize = std::max(1, std::stoi(argv[6]));
+        if (argc > 7) maxDetections = std::max(100, std::stoi(argv[7]));
+        if (argc > 8) benchmarkRuns = std::max(0, std::stoi(argv[8]));
+    } catch (...) {
+        std::cerr << "[ERR] Invalid numeric argument\n";
+        return 1;
+    }
+
+    int winW = 0, winH = 0;
+    int64_t nf = 0, ns = 0, nst = 0;
+    if (vj_model_load_header(modelPath.c_str(), &winW, &winH, &nf, &ns, &nst) != VJ_OK) {
+        std::cerr << "[ERR] loadCascadeModel failed: " << modelPath << " (" << vj_last_error() << ")\n";
+        return 1;
+    }
+    std::vector<vj_haar_feature> feats(static_cast<size_t>(nf));
+    std::vector<vj_stump4> stumps(static_cast<size_t>(ns));
+    std::vector<vj_cascade_stage> stages(static_cast<size_t>(nst));
+    if (vj_model_load(modelPath.c_str(), feats.data(), nf, stumps.data(), ns, stages.data(), nst) != VJ_OK) {
+        std::cerr << "[ERR] loadCascadeModel failed: " << modelPath << " (" << vj_last_error() << ")\n";
+        return 1;
+    }
+    Gray img;
+    if (!load_pgm(imagePath, img)) return 1;
+
+    vj_detector* det = nullptr;
+    if (vj_detector_create(winW, winH, std::max(winW, img.w), std::max(winH, img.h), maxDetections, &det) != VJ_OK)
+        return fail("detector create");
+    if (vj_detector_set_model(det, feats.data(), nf, stumps.data(), ns, stages.data(), nst) != VJ_OK)
+        return fail("setCascadeModel");
+    // The reference uploads the image once and detects from device memory.
+    uint8_t* dImage = nullptr;
+    if (cudaMalloc(&dImage, img.px.size()) != cudaSuccess ||
+        cudaMemcpy(dImage, img.px.data(), img.px.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        std::cerr << "[ERR] cudaMemcpy to device failed\n";
+        return 1;
+    }
+    std::vector<vj_detection> dets(static_cast<size_t>(maxDetections));
+    int count = 0;
+    auto detect = [&]() {
+        return vj_detect(det, dImage, img.w, img.h, img.w, 1, scaleFactor, minNeighbors, minObjectSize, maxDetections,
+                         1, dets.data(), maxDetections, &count, nullptr);
+    };
+    if (benchmarkRuns > 0) {
+        for (int i = 0; i < 3; ++i)
+            if (detect() != VJ_OK) return fail("warmup detectMultiScale");
+        double sum = 0.0, mn = std::numeric_limits<double>::infinity(), mx = 0.0;
+        for (int i = 0; i < benchmarkRuns; ++i) {
+            const auto t0 = std::chrono::steady_clock::now();
+            if (detect() != VJ_OK) return fail("detectMultiScale");
+            const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            sum += ms;
+            mn = std::min(mn, ms);
+            mx = std::max(mx, ms);
+        }
+        const double avg = sum / benchmarkRuns;
+        std::cout << "[DETECT_BENCH] runs=" << benchmarkRuns << " detections(last)=" << count << " avg(ms): " << avg
+                  << " min(ms): " << mn << " max(ms): " << mx << " avg(fps): " << (avg > 0.0 ? 1000.0 / avg : 0.0)
+                  << "\n";
+    } else {
+        const auto t0 = std::chrono::high_resolution_clock::now();
+        if (detect() != VJ_OK) return fail("detectMultiScale");
+        const auto ms =
+            std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::high_resolution_clock::now() - t0)
+                .count();
+        std::cout << "[DETECT] detections=" << count << " elapsed(ms): " << ms << "\n";
+    }
+    std::vector<uint8_t> rgb(static_cast<size_t>(img.w) * img.h * 3);
+    for (size_t i = 0; i < img.px.size(); ++i) rgb[3 * i] = rgb[3 * i + 1] = rgb[3 * i + 2] = img.px[i];
+    for (int i = 0; i < count; ++i) draw_frame(rgb, img.w, img.h, dets[static_cast<size_t>(i)]);
+    cudaFree(dImage);
+    vj_detector_destroy(det);
+    if (!save_ppm(outPath, img.w, img.h, rgb)) {
+        std::cerr << "[ERR] savePPM failed\n";
+        return 1;
+    }
+    std::cout << "[OK] Saved result to: " << outPath << "\n";
+    return 0;
+}

@@ -420,7 +420,11 @@ typedef struct vj_detect_config {
     int32_t queueStumps;  /* lane-per-window queue passes then cover at least
                              this many more stumps (0 = none) before the
                              warp-per-window deep pass takes the rest */
-    int32_t blocksPerSM;  /* persistent CTAs per SM; 0 = as many as fit */
+    int32_t blocksPerSM;  /* persistent CTAs per SM (0 = as many as fit); 4 or
+                             more selects the kernel compiled for 4 CTAs per
+                             SM (64 registers per thread) */
+    int32_t deepSlots;    /* windows a warp holds in the deep pass: 2 or 4 */
+    int32_t reserved;     /* 0 */
 } vj_detect_config;
 
 int vj_detector_set_config(vj_detector* d, const vj_detect_config* cfg);
