@@ -94,10 +94,12 @@ def build_tools(verbose: bool = False, force: bool = False) -> list[Path]:
     cuda_lib = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "lib64"
     out = []
     procs = []
+    newest = max([LIB.stat().st_mtime] + [h.stat().st_mtime for h in TOOLS.glob("*.h")] +
+                 [h.stat().st_mtime for h in INCLUDE.glob("*.h")])
     for src in sorted(TOOLS.glob("*.cpp")):
         exe = BIN / src.stem
         out.append(exe)
-        if not force and exe.exists() and exe.stat().st_mtime > max(src.stat().st_mtime, LIB.stat().st_mtime):
+        if not force and exe.exists() and exe.stat().st_mtime > max(src.stat().st_mtime, newest):
             continue
         cmd = [CXX, *CXXFLAGS, "-I", str(INCLUDE), "-I", "/usr/local/cuda/include", str(src), "-o", str(exe),
                "-L", str(PKG), "-lvjgb", "-L", str(cuda_lib), "-lcudart", "-Wl,-rpath,$ORIGIN/..", "-lpthread"]

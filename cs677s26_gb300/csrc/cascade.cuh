@@ -315,6 +315,53 @@ __device__ __forceinline__ float stage_sum(const DStump* __restrict__ stumps, co
     return acc;
 }
 
+// A stump decoded for one level: corner offsets dy * pitch + dx relative to
+// the window origin, weights, rectangle count, threshold and leaf values.
+struct LevelStump {
+    int off[12];
+    float w[3];
+    int nr;
+    float theta, left, right;
+};
+
+__device__ __forceinline__ void decode_stump(const DStump* __restrict__ sp, int pitch, LevelStump& d) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(sp));
+    const float4 wv = __ldg(reinterpret_cast<const float4*>(sp) + 1);
+    const int4 dd = __ldg(reinterpret_cast<const int4*>(sp) + 2);
+    const int4 ee = __ldg(reinterpret_cast<const int4*>(sp) + 3);
+    d.theta = a.x;
+    d.left = a.y;
+    d.right = a.z;
+    d.nr = __float_as_int(a.w);
+    d.w[0] = wv.x;
+    d.w[1] = wv.y;
+    d.w[2] = wv.z;
+    const uint32_t dxw[3] = {static_cast<uint32_t>(dd.x), static_cast<uint32_t>(dd.y), static_cast<uint32_t>(dd.z)};
+    const uint32_t dyw[3] = {static_cast<uint32_t>(dd.w), static_cast<uint32_t>(ee.x), static_cast<uint32_t>(ee.y)};
+#pragma unroll
+    for (int ci = 0; ci < 12; ++ci) {
+        const int dx = static_cast<int8_t>((dxw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
+        const int dy = static_cast<int8_t>((dyw[ci >> 2] >> (8 * (ci & 3))) & 0xFFu);
+        d.off[ci] = dy * pitch + dx;
+    }
+}
+
+// Leaf value of a decoded stump for the window at integral offset b; the same
+// operations in the same order as stump_value.
+__device__ __forceinline__ float decoded_value(const LevelStump& d, const uint32_t* sum, int b, float inv) {
+    float raw = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        if (r < d.nr) {
+            const float c0 = corner_f(sum[b + d.off[4 * r]]), c1 = corner_f(sum[b + d.off[4 * r + 1]]);
+            const float c2 = corner_f(sum[b + d.off[4 * r + 2]]), c3 = corner_f(sum[b + d.off[4 * r + 3]]);
+            const float v = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(c0, c1), c2), c3), d.w[r]);
+            raw = (r == 0) ? v : __fadd_rn(raw, v);
+        }
+    }
+    return __fmul_rn(raw, inv) < d.theta ? d.left : d.right;
+}
+
 // Leaf value of stump k from the window's integral patch in shared memory
 // (corners already converted to float).
 __device__ __forceinline__ float patch_stump_value(const PStumpPlanes& ps, int k, const float* patch, float inv) {
@@ -418,9 +465,11 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
         if (lane == 0) t = atomicAdd(workCounter, 1ull);
         t = __shfl_sync(0xffffffffu, t, 0);
         int count = 0;
+        int tileLevel = -1;  // the level of every window in the list (tile pass)
         if (qin == nullptr) {
             if (t >= static_cast<unsigned long long>(P.totalTiles)) break;
             const int li = find_level(P.levels, P.nLevels, static_cast<int64_t>(t));
+            tileLevel = li;
             const CasLevel L = P.levels[li];
             const int64_t local = static_cast<int64_t>(t) - L.tileBase;
             const int tx = static_cast<int>(local % L.tilesX), ty = static_cast<int>(local / L.tilesX);
@@ -453,7 +502,63 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
             for (int i = lane; i < count; i += 32) lst[i] = qin[base + i];
         }
         __syncwarp();
-        for (int si = s0; si < s1 && count > 0; ++si) {
+        if (tileLevel >= 0) {
+            // One level for the whole list: every stump is decoded once for up
+            // to 128 windows (4 per lane), whose integral loads are then in
+            // flight together.  Each window's sum still adds its stumps in
+            // order from 0.0f.
+            const CasLevel& L = P.levels[tileLevel];
+            const uint32_t* sum = L.sum;
+            const int pitch = static_cast<int>(L.pitch);
+            for (int si = s0; si < s1 && count > 0; ++si) {
+                const DStage st = P.stages[si];
+                evals += static_cast<unsigned long long>(count) * static_cast<unsigned>(st.ntrees);
+                int nc = 0;
+                for (int g0 = 0; g0 < count; g0 += 128) {
+                    const int ng = min(4, (count - g0 + 31) >> 5);  // groups of 32 in this block
+                    int b[4];
+                    float inv[4], acc[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int i = g0 + 32 * q + lane;
+                        b[q] = 0;
+                        inv[q] = 0.0f;
+                        acc[q] = 0.0f;
+                        if (q < ng && i < count) {
+                            const QEntry e = lst[i];
+                            b[q] = static_cast<int>(e.xy >> 16) * pitch + static_cast<int>(e.xy & 0xFFFFu);
+                            inv[q] = e.inv;
+                        }
+                    }
+                    for (int k = 0; k < st.ntrees; ++k) {
+                        LevelStump d;
+                        decode_stump(P.stumps + st.first + k, pitch, d);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (q < ng) acc[q] = __fadd_rn(acc[q], decoded_value(d, sum, b[q], inv[q]));
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (q >= ng) break;
+                        const int i = g0 + 32 * q + lane;
+                        const bool act = i < count;
+                        QEntry e{};
+                        if (act) e = lst[i];
+                        const bool pass = act && !(acc[q] < st.threshold);
+                        const unsigned m = __ballot_sync(0xffffffffu, pass);
+                        __syncwarp();
+                        if (pass) {
+                            e.score = acc[q];
+                            lst[nc + __popc(m & lanemask_lt())] = e;
+                        }
+                        nc += __popc(m);
+                        __syncwarp();
+                    }
+                }
+                count = nc;
+            }
+        }
+        for (int si = s0; si < s1 && count > 0 && tileLevel < 0; ++si) {
             const DStage st = P.stages[si];
             evals += static_cast<unsigned long long>(count) * static_cast<unsigned>(st.ntrees);
             int nc = 0;

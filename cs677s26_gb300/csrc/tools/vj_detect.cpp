@@ -21,106 +21,15 @@
 
 #include <cuda_runtime.h>
 
+#include "image_io.h"
 #include "vjgb.h"
 
 namespace {
 
-struct Gray {
-    int w = 0, h = 0;
-    std::vector<uint8_t> px;
-};
-
-// Next header token, skipping whitespace and '#' comment lines.
-bool next_token(std::istream& is, std::string& tok) {
-    tok.clear();
-    while (is.good()) {
-        const int c = is.peek();
-        if (c == '#') {
-            std::string line;
-            std::getline(is, line);
-            continue;
-        }
-        if (c != EOF && std::isspace(static_cast<unsigned char>(c))) {
-            is.get();
-            continue;
-        }
-        break;
-    }
-    if (!is.good()) return false;
-    is >> tok;
-    return !tok.empty();
-}
-
-// Binary P5 PGM with maxval <= 255.
-bool load_pgm(const std::string& path, Gray& g) {
-    std::ifstream ifs(path, std::ios::binary);
-    if (!ifs) {
-        std::cerr << "[ERR] Cannot open PGM: " << path << "\n";
-        return false;
-    }
-    std::string tok;
-    if (!next_token(ifs, tok) || tok != "P5") {
-        std::cerr << "[ERR] Unsupported PGM format (need P5): " << path << "\n";
-        return false;
-    }
-    int maxVal = 0;
-    try {
-        if (!next_token(ifs, tok)) return false;
-        g.w = std::stoi(tok);
-        if (!next_token(ifs, tok)) return false;
-        g.h = std::stoi(tok);
-        if (!next_token(ifs, tok)) return false;
-        maxVal = std::stoi(tok);
-    } catch (...) {
-        std::cerr << "[ERR] Invalid PGM metadata\n";
-        return false;
-    }
-    if (g.w <= 0 || g.h <= 0 || maxVal <= 0 || maxVal > 255) {
-        std::cerr << "[ERR] Invalid PGM metadata\n";
-        return false;
-    }
-    ifs.get();  // the single whitespace after the header
-    g.px.resize(static_cast<size_t>(g.w) * g.h);
-    if (!ifs.read(reinterpret_cast<char*>(g.px.data()), static_cast<std::streamsize>(g.px.size()))) {
-        std::cerr << "[ERR] Failed to read PGM pixel payload\n";
-        return false;
-    }
-    return true;
-}
-
-bool save_ppm(const std::string& path, int w, int h, const std::vector<uint8_t>& rgb) {
-    std::ofstream ofs(path, std::ios::binary);
-    if (!ofs) {
-        std::cerr << "[ERR] Cannot write PPM: " << path << "\n";
-        return false;
-    }
-    ofs << "P6\n" << w << " " << h << "\n255\n";
-    ofs.write(reinterpret_cast<const char*>(rgb.data()), static_cast<std::streamsize>(rgb.size()));
-    return static_cast<bool>(ofs);
-}
-
-// 2-pixel white frame, clipped to the image.
-void draw_frame(std::vector<uint8_t>& rgb, int w, int h, const vj_detection& d) {
-    const int x0 = std::max(0, d.x), y0 = std::max(0, d.y);
-    const int x1 = std::min(w - 1, d.x + d.w - 1), y1 = std::min(h - 1, d.y + d.h - 1);
-    if (x0 > x1 || y0 > y1) return;
-    auto set = [&](int x, int y) {
-        const size_t i = (static_cast<size_t>(y) * w + x) * 3;
-        rgb[i] = rgb[i + 1] = rgb[i + 2] = 255;
-    };
-    for (int t = 0; t < 2; ++t) {
-        const int yt = std::min(h - 1, y0 + t), yb = std::max(0, y1 - t);
-        for (int x = x0; x <= x1; ++x) {
-            set(x, yt);
-            set(x, yb);
-        }
-        const int xl = std::min(w - 1, x0 + t), xr = std::max(0, x1 - t);
-        for (int y = y0; y <= y1; ++y) {
-            set(xl, y);
-            set(xr, y);
-        }
-    }
-}
+using vjtools::Gray;
+using vjtools::draw_frame;
+using vjtools::load_pgm;
+using vjtools::save_ppm;
 
 int fail(const char* what) {
     std::cerr << "[ERR] " << what << " failed: " << vj_last_error() << "\n";

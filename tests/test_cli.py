@@ -81,3 +81,63 @@ def test_vj_detect_writes_the_reference_image(cuda, vj, basic_pool, model_file, 
     r = subprocess.run([str(EXE), str(path), str(pgm), str(ppm), "1.25", "4", "24", "200000", "2"],
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "[DETECT_BENCH] runs=2" in r.stdout
+
+
+TRAIN = ROOT / "cs677s26_gb300" / "bin" / "vj_train"
+
+
+def test_vj_train_arguments(tmp_path):
+    r = subprocess.run([str(TRAIN)], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage: vj_train" in r.stderr
+    r = subprocess.run([str(TRAIN), str(tmp_path / "m.bin")], capture_output=True, text=True)
+    assert r.returncode == 1 and "stageNegCacheDir is required" in r.stderr
+    args = [str(tmp_path / "faces.bin"), "10000", "250", "200000", "4", "1.0", str(tmp_path / "m.bin")]
+    r = subprocess.run([str(TRAIN)] + args, capture_output=True, text=True)
+    assert r.returncode == 1 and "scaleFactor must be > 1.0" in r.stderr
+    (tmp_path / "faces.bin").write_bytes(bytes(100))
+    args = [str(tmp_path / "faces.bin"), "10000", "250", "200000", "4", "1.25", "38", "0.99", "0.4", "24",
+            str(tmp_path), str(tmp_path), "677", "3", str(tmp_path / "m.bin")]
+    r = subprocess.run([str(TRAIN)] + args, capture_output=True, text=True)
+    assert r.returncode == 1 and "not divisible by samplePixels" in r.stderr
+
+
+@pytest.mark.gpu
+def test_vj_train_small_cascade(cuda, vj, oracle, tmp_path):
+    """A short training run on synthetic data: the stage-0 training set it
+    dumps gives, through the oracle's restatement of runCpuWeakSearch over the
+    Core pool, the first weak classifier the run reports; the saved model
+    loads and detects."""
+    faces = vj.synth_patches(11, 2000, 0)
+    (tmp_path / "faces.bin").write_bytes(faces.tobytes())
+    negdir = tmp_path / "neg"
+    negdir.mkdir()
+    for k in range(24):
+        write_pgm(negdir / f"n{k:02d}.pgm", vj.synth_scene(700 + k, 320 + 16 * k, 240 + 8 * k, 0, 24, 100))
+    dump = tmp_path / "dump"
+    dump.mkdir()
+    model = tmp_path / "model.bin"
+    args = [str(tmp_path / "faces.bin"), "10000", "4", "200000", "4", "1.25", "3", "0.95", "0.8", "24",
+            str(tmp_path), str(negdir), "677", "3", str(model)]
+    env = dict(__import__("os").environ, VJ_TRAIN_DUMP=str(dump))
+    r = subprocess.run([str(TRAIN)] + args, capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "[OK] Saved model to:" in r.stdout
+    first = [ln for ln in r.stdout.splitlines() if ln.startswith("[TRAIN] stage=0 weak=0 ")][0]
+    fields = dict(kv.split("=", 1) for kv in first.split()[1:] if "=" in kv)
+    # stage 0 set: 2000 positives then 10000 negatives, weights 0.5/n normalised
+    raw = np.frombuffer((dump / "stage00.bin").read_bytes(), np.uint8).reshape(-1, 24, 24)
+    assert raw.shape[0] == 12000 and np.array_equal(raw[:2000], faces)
+    labels = np.array([1] * 2000 + [-1] * 10000, np.int8)
+    w = np.where(labels > 0, np.float32(0.5) / np.float32(2000), np.float32(0.5) / np.float32(10000))
+    w = (w.astype(np.float64) / w.astype(np.float64).sum()).astype(np.float32)
+    sums, inv = oracle.train_integrals(raw)
+    core = np.ascontiguousarray(vj.feature_pool(vj.FeatureMode.Core)).view(oracle.FEATURE)
+    best = oracle.weak_search(core, sums, inv, labels, w, threads=16)
+    assert int(fields["feature"]) == best["featureIdx"]
+    assert int(fields["parity"]) == best["parity"]
+    feats, stumps, stages = vj.ModelIO.loadCascadeModel(str(model))[1:4]
+    assert len(stages) >= 1 and len(feats) == 210400
+    pgm, ppm = tmp_path / "s.pgm", tmp_path / "s.ppm"
+    write_pgm(pgm, vj.synth_scene(9, 640, 480, 4, 24, 200))
+    r = subprocess.run([str(EXE), str(model), str(pgm), str(ppm)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "[DETECT] detections=" in r.stdout
