@@ -105,6 +105,7 @@ SIGNATURES = {
     "vj_group_rectangles": (i32, [vp, i32, i32, f32, vp, pi32]),
     "vj_detect_batch": (i32, [vp, i32, vp, vp, vp, vp, i32, f32, i32, i32, i32, i32, vp, i32, vp, vp]),
     "vj_detector_last_stats": (i32, [vp, vp]),
+    "vj_detector_test_barrier_timeout": (i32, [vp, i32, i64]),
     "vj_detector_set_config": (i32, [vp, vp]),
     "vj_detector_get_config": (i32, [vp, vp]),
     "vj_detector_autotune": (i32, [vp, i32, vp, vp, vp, vp, i32, f32, i32, i32, vp, vp]),

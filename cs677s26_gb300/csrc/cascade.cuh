@@ -111,7 +111,11 @@ struct DevPlan {
     int winW, winH, normMode, nStages;
     int tileStages, deepFrom, qcap, detCap;
     int queueEnd[kMaxQueuePasses];  // stage range of queue pass m: [m ? queueEnd[m-1] : tileStages, queueEnd[m])
-    int hostCap, pad0;
+    int hostCap;
+    // Wait tests: when >= 0, this block leaves before the first grid barrier,
+    // so the others' wait runs out after barrierTimeoutNs.
+    int holdBlock;
+    unsigned long long barrierTimeoutNs;  // 0 = kBarrierTimeoutNs
     int64_t totalTiles;
     IIPlan ip;
     const int* rjFirst;         // nResize + 1: resize jobs of chain position p
@@ -155,7 +159,7 @@ constexpr unsigned kBarrierMaxSpins = 1u << 30;
 // count, after which the error flag is set.  Returns false (in every thread of
 // the block) once any block has set the error flag, so all blocks leave the
 // kernel instead of waiting again.
-__device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned& epoch) {
+__device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned& epoch, unsigned long long timeoutNs) {
     __shared__ int okShared;
     __syncthreads();
     ++epoch;
@@ -171,7 +175,7 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned& epoch) {
                 ok = false;
                 break;
             }
-            if ((it & 127u) == 127u && (global_ns() - t0 > kBarrierTimeoutNs || it > kBarrierMaxSpins)) {
+            if ((it & 127u) == 127u && (global_ns() - t0 > timeoutNs || it > kBarrierMaxSpins)) {
                 atomicExch(&g->error, 1u);
                 ok = false;
                 break;
@@ -731,26 +735,28 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     const bool stamper = blockIdx.x == 0 && threadIdx.x == 0;
+    const unsigned long long tmo = P.barrierTimeoutNs ? P.barrierTimeoutNs : kBarrierTimeoutNs;
     if (stamper) G->stamp[0] = global_ns();
+    if (P.holdBlock >= 0 && blockIdx.x == static_cast<unsigned>(P.holdBlock)) return;
 
     // 1. pyramid
     for (int p = 0; p < P.nResize; ++p) {
         const int j0 = P.rjFirst[p], j1 = P.rjFirst[p + 1];
         const int64_t items = P.rjItems[p];
         for (int64_t it = gw; it < items; it += nw) resize_item(P.rjobs + j0, j1 - j0, it, lane);
-        if (!grid_barrier(G, epoch)) return;
+        if (!grid_barrier(G, epoch, tmo)) return;
     }
     if (stamper) G->stamp[1] = global_ns();
 
     // 2. integral images
     for (int64_t r = gw; r < P.ip.rows; r += nw) ii_row_item(P.iijobs, P.nLevels, r, lane);
-    if (!grid_barrier(G, epoch)) return;
+    if (!grid_barrier(G, epoch, tmo)) return;
     for (int64_t it = gw; it < P.ip.items; it += nw)
         ii_col_total_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
-    if (!grid_barrier(G, epoch)) return;
+    if (!grid_barrier(G, epoch, tmo)) return;
     for (int64_t it = gw; it < P.ip.items; it += nw)
         ii_col_scan_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
-    if (!grid_barrier(G, epoch)) return;
+    if (!grid_barrier(G, epoch, tmo)) return;
     if (stamper) G->stamp[2] = global_ns();
 
     unsigned long long gated = 0, evals = 0, deepEvals = 0;
@@ -758,7 +764,7 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
 
     // 3. tile pass -> queue 0 (or detections)
     lane_pass<TH>(P, lst, nullptr, 0, 0, P.tileStages, &C->work[0], P.q[0], &C->qcount[0], gated, evals);
-    if (!grid_barrier(G, epoch)) return;
+    if (!grid_barrier(G, epoch, tmo)) return;
     if (stamper) G->stamp[3] = global_ns();
 
     // 4. queue passes: queue m -> queue m+1
@@ -767,7 +773,7 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
         const int nIn = min(C->qcount[m], P.qcap);
         lane_pass<TH>(P, lst, P.q[m & 1], nIn, s0, P.queueEnd[m], &C->work[1 + m], P.q[(m + 1) & 1],
                       &C->qcount[m + 1], gated, evals);
-        if (!grid_barrier(G, epoch)) return;
+        if (!grid_barrier(G, epoch, tmo)) return;
     }
     if (stamper) G->stamp[4] = global_ns();
 
@@ -788,7 +794,7 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
         if (gated) atomicAdd(&C->stats[0], gated);
         if (evals + deepSum) atomicAdd(&C->stats[1], evals + deepSum);
     }
-    if (!grid_barrier(G, epoch)) return;
+    if (!grid_barrier(G, epoch, tmo)) return;
     if (stamper) G->stamp[5] = global_ns();
 
     // 6. compaction: block 0 lays out the images' raw detections in the host
@@ -819,7 +825,7 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
             off += min(P.counts[i], P.detCap);
         }
     }
-    if (!grid_barrier(G, epoch)) return;
+    if (!grid_barrier(G, epoch, tmo)) return;
     if (C->compactOverflow == 0) {
         for (int64_t i = gw; i < P.nImg; i += nw) {
             const int cnt = min(P.counts[i], P.detCap);

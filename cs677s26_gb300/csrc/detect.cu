@@ -199,6 +199,10 @@ struct vj_detector {
     int detHint = 0;
     int64_t hostHint = 0;
     vj_detect_stats stats{};
+    // Wait test (vj_detector_test_barrier_timeout): one block leaves before
+    // the first grid barrier and the others wait at most this long.
+    int testHoldBlock = -1;
+    unsigned long long testBarrierTimeoutNs = 0;
 };
 
 namespace {
@@ -570,6 +574,8 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         P.detCap = detCap;
         for (size_t m = 0; m < D->queueEnds.size(); ++m) P.queueEnd[m] = D->queueEnds[m];
         P.hostCap = static_cast<int>(std::min<int64_t>(hostCap, INT32_MAX));
+        P.holdBlock = D->testHoldBlock;
+        P.barrierTimeoutNs = D->testBarrierTimeoutNs;
         P.totalTiles = tiles;
         P.ip = ip;
         P.rjFirst = reinterpret_cast<const int*>(dp + oFirst);
@@ -660,12 +666,15 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
     const int nImg = static_cast<int>(ims.size());
     const int limit = std::max(1, maxDet);
     const vj_detection* hd = D->hdets.as<vj_detection>();
+    const int hw = std::max(1, static_cast<int>(std::thread::hardware_concurrency()));
+    // batches post-process images in parallel; a few images use the threads inside grouping
+    const int groupThreads = nImg >= 8 ? 1 : std::min(8, hw);
     auto post = [&](int i) {
         const vj_detection* src = hd + ho[i];
         std::vector<vj_detection> raw(src, src + std::min(hc[i], detCap));
         canonical_sort(raw);
         if (static_cast<int>(raw.size()) > limit) raw.resize(limit);
-        std::vector<vj_detection> res = group ? group_rectangles(raw, minN, 0.2f) : std::move(raw);
+        std::vector<vj_detection> res = group ? group_rectangles(raw, minN, 0.2f, groupThreads) : std::move(raw);
         const int k = std::min(static_cast<int>(res.size()), capPer);
         if (k > 0) std::memcpy(out + static_cast<size_t>(i) * capPer, res.data(), sizeof(vj_detection) * k);
         counts[i] = k;
@@ -938,6 +947,14 @@ int vj_detect_batch(vj_detector* d, int n, const uint8_t* const* images, const i
     st = run_batch(d, ims, images_on_device != 0, scaleFactor, minNeighbors, minObjectSize, maxDet,
                    applyGrouping != 0, out, capPerImage, counts, static_cast<cudaStream_t>(stream));
     return st == VJ_OK ? ok() : st;
+}
+
+int vj_detector_test_barrier_timeout(vj_detector* d, int holdBlock, int64_t timeoutNs) {
+    if (!d || holdBlock < -1 || timeoutNs < 0)
+        return set_error(VJ_INVALID_ARG, "vj_detector_test_barrier_timeout: bad arguments");
+    d->testHoldBlock = holdBlock;
+    d->testBarrierTimeoutNs = static_cast<unsigned long long>(timeoutNs);
+    return ok();
 }
 
 int vj_detector_last_stats(const vj_detector* d, vj_detect_stats* out) {

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <thread>
 
 namespace vjgb {
 namespace {
@@ -84,7 +85,8 @@ void canonical_sort(std::vector<vj_detection>& v) {
     v.swap(out);
 }
 
-std::vector<vj_detection> group_rectangles(const std::vector<vj_detection>& in, int minNeighbors, float eps) {
+std::vector<vj_detection> group_rectangles(const std::vector<vj_detection>& in, int minNeighbors, float eps,
+                                           int threads) {
     const int n = static_cast<int>(in.size());
     if (n == 0) return {};
     std::vector<int> parent(n), rnk(n, 0), order;
@@ -116,37 +118,58 @@ std::vector<vj_detection> group_rectangles(const std::vector<vj_detection>& in, 
         sw[k] = d.w;
         sh[k] = d.h;
     }
-    std::vector<int> cand(static_cast<size_t>(n));
-    for (int oi = 0; oi < n; ++oi) {
-        const int ax = sx[oi], ay = sy[oi], aw = sw[oi], ah = sh[oi];
-        const int reach = static_cast<int>(eps * static_cast<float>(aw + ah) * 0.5f);
-        const int end = static_cast<int>(std::upper_bound(sx.begin() + oi + 1, sx.end(), ax + reach) - sx.begin());
-        // Candidates in the x window whose y distance is within the reach
-        // (|dy| <= delta <= reach is necessary): a bit mask per 64 rectangles,
-        // then the set bits in increasing order.
-        int nc = 0;
-        const unsigned span = 2u * static_cast<unsigned>(reach);
-        const int* yv = sy.data();
-        for (int base = oi + 1; base < end; base += 64) {
-            const int lim = std::min(64, end - base);
-            uint64_t m = 0;
-            for (int k = 0; k < lim; ++k)
-                m |= static_cast<uint64_t>(static_cast<unsigned>(yv[base + k] - ay + reach) <= span) << k;
-            while (m) {
-                cand[static_cast<size_t>(nc++)] = base + __builtin_ctzll(m);
-                m &= m - 1;
+    // The similar pairs of sweep positions [o0, o1), in sweep order: the
+    // (oi, oj) sequence whose unions the reference performs.
+    auto sweep = [&](int o0, int o1, auto&& emit) {
+        std::vector<int> cand;
+        for (int oi = o0; oi < o1; ++oi) {
+            const int ax = sx[oi], ay = sy[oi], aw = sw[oi], ah = sh[oi];
+            const int reach = static_cast<int>(eps * static_cast<float>(aw + ah) * 0.5f);
+            const int end = static_cast<int>(std::upper_bound(sx.begin() + oi + 1, sx.end(), ax + reach) - sx.begin());
+            // Candidates in the x window whose y distance is within the reach
+            // (|dy| <= delta <= reach is necessary): a bit mask per 64
+            // rectangles, then the set bits in increasing order.
+            cand.clear();
+            const unsigned span = 2u * static_cast<unsigned>(reach);
+            const int* yv = sy.data();
+            for (int base = oi + 1; base < end; base += 64) {
+                const int lim = std::min(64, end - base);
+                uint64_t m = 0;
+                for (int k = 0; k < lim; ++k)
+                    m |= static_cast<uint64_t>(static_cast<unsigned>(yv[base + k] - ay + reach) <= span) << k;
+                while (m) {
+                    cand.push_back(base + __builtin_ctzll(m));
+                    m &= m - 1;
+                }
+            }
+            for (const int oj : cand) {
+                const int bx = sx[oj];
+                const int dy = ay - sy[oj];
+                const int bw = sw[oj], bh = sh[oj];
+                const int delta =
+                    static_cast<int>(eps * static_cast<float>(std::min(aw, bw) + std::min(ah, bh)) * 0.5f);
+                if (std::abs(ax - bx) <= delta && std::abs(dy) <= delta && std::abs(ax + aw - bx - bw) <= delta &&
+                    std::abs(ay + ah - sy[oj] - bh) <= delta)
+                    emit(order[oi], order[oj]);
             }
         }
-        for (int c = 0; c < nc; ++c) {
-            const int oj = cand[static_cast<size_t>(c)];
-            const int bx = sx[oj];
-            const int dy = ay - sy[oj];
-            const int bw = sw[oj], bh = sh[oj];
-            const int delta = static_cast<int>(eps * static_cast<float>(std::min(aw, bw) + std::min(ah, bh)) * 0.5f);
-            if (std::abs(ax - bx) <= delta && std::abs(dy) <= delta && std::abs(ax + aw - bx - bw) <= delta &&
-                std::abs(ay + ah - sy[oj] - bh) <= delta)
-                unite(order[oi], order[oj]);
-        }
+    };
+    const int T = (threads > 1 && n >= 4096) ? std::min(threads, 16) : 1;
+    std::vector<std::vector<std::pair<int, int>>> pairs(static_cast<size_t>(T));
+    if (T == 1) {
+        sweep(0, n, unite);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < T; ++t)
+            th.emplace_back([&, t] {
+                auto& part = pairs[static_cast<size_t>(t)];
+                sweep(static_cast<int>(static_cast<int64_t>(n) * t / T),
+                      static_cast<int>(static_cast<int64_t>(n) * (t + 1) / T),
+                      [&part](int a, int b) { part.emplace_back(a, b); });
+            });
+        for (auto& x : th) x.join();
+        for (const auto& part : pairs)
+            for (const auto& pr : part) unite(pr.first, pr.second);
     }
     struct Acc {
         int64_t x = 0, y = 0, w = 0, h = 0;

@@ -410,6 +410,14 @@ typedef struct vj_detect_stats {
 
 int vj_detector_last_stats(const vj_detector* d, vj_detect_stats* out);
 
+/* Failure-path test of the detection kernel's grid barrier (no reference
+ * counterpart): while holdBlock >= 0, that block of the next launches leaves
+ * the kernel before the first barrier, and the other blocks' wait for it runs
+ * out after timeoutNs (0 = the normal 60 s limit); the call then returns
+ * VJ_RUNTIME_ERROR and the context stays usable.  holdBlock -1 restores
+ * normal launches. */
+int vj_detector_test_barrier_timeout(vj_detector* d, int holdBlock, int64_t timeoutNs);
+
 /* Launch shape of the detection kernel (no reference counterpart).  Every
  * configuration gives the same detections; they differ only in speed. */
 typedef struct vj_detect_config {

@@ -133,3 +133,22 @@ def test_reserved_arena(cuda, vj, basic_pool, full_case):
     assert e.reserve(0) == 0  # back to buffers grown on demand
     s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
     assert s == 0 and raw.tobytes() == ref.tobytes()
+
+
+def test_barrier_wait_runs_out_and_context_survives(cuda, vj, basic_pool, full_case):
+    """A grid-barrier wait that cannot finish (one block leaves before the
+    first barrier) ends after its short limit with VJ_RUNTIME_ERROR; the next
+    launch on the same context gives the oracle's detections."""
+    import time
+    st, sg, scene, ref = full_case
+    e = engine(vj, basic_pool, st, sg)
+    lib = vj.load()
+    h, w = scene.shape
+    assert lib.vj_detector_test_barrier_timeout(e._h, 5, 2_000_000) == 0
+    t0 = time.time()
+    s, _ = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == vj.Status.kRuntimeError and time.time() - t0 < 30
+    assert b"barrier" in lib.vj_last_error()
+    assert lib.vj_detector_test_barrier_timeout(e._h, -1, 0) == 0
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0 and raw.tobytes() == ref.tobytes()
