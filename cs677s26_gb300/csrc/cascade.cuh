@@ -654,8 +654,17 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
             const int64_t Pi = L.pitch;
             const int64_t b = static_cast<int64_t>(ne.xy >> 16) * Pi + static_cast<int64_t>(ne.xy & 0xFFFFu);
             float* dst = patches + s * pe;
-            for (int r = 0; r < ph; ++r)
-                for (int c = lane; c < pw; c += 32) dst[r * pw + c] = corner_f(sum[b + r * Pi + c]);
+            // 8 rows' loads in flight before their stores
+            for (int c = lane; c < pw; c += 32)
+                for (int r0 = 0; r0 < ph; r0 += 8) {
+                    uint32_t v[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (r0 + k < ph) v[k] = sum[b + (r0 + k) * Pi + c];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (r0 + k < ph) dst[(r0 + k) * pw + c] = corner_f(v[k]);
+                }
             if (slot == s) {
                 qi = static_cast<int>(t);
                 e = ne;
