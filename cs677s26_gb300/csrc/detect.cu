@@ -179,7 +179,7 @@ struct vj_detector {
     // range of it, so the detector never holds more than its reservation.
     DBuf arena;
     // Launch shape and the stage schedule derived from it.
-    vj_detect_config cfg{8, 64, 0, 4, 2, 0};
+    vj_detect_config cfg{8, 64, 0, 0, 2, 0};
     int tileStages = 0, deepFrom = 0;
     std::vector<int> queueEnds;
     // Launch graph and what it was built for.
