@@ -38,7 +38,7 @@ STAGE_CALIB = np.dtype([("cutVal", "<f4"), ("stageThreshold", "<f4"), ("strictGt
 
 DETECT_STATS = np.dtype([("images", "<i8"), ("levels", "<i8"), ("pyramidPixels", "<i8"), ("windows", "<i8"),
                          ("gated", "<i8"), ("stumpEvals", "<i8"), ("rawDetections", "<i8"), ("deepWindows", "<i8"),
-                         ("attempts", "<i4"), ("queuePasses", "<i4"), ("gpuMs", "<f8"), ("phaseMs", "<f8", 6),
+                         ("attempts", "<i4"), ("queuePasses", "<i4"), ("gpuMs", "<f8"), ("phaseMs", "<f8", 7),
                          ("hostMs", "<f8", 3)])
 DETECT_CONFIG = np.dtype([("tileRows", "<i4"), ("tileStumps", "<i4"), ("queueStumps", "<i4"), ("blocksPerSM", "<i4"),
                           ("deepSlots", "<i4"), ("reserved", "<i4")])
@@ -51,10 +51,10 @@ SERVER_STATS = np.dtype([("submitted", "<i8"), ("completed", "<i8"), ("failed", 
                          ("meanBatchImages", "<f8"), ("meanMs", "<f8"), ("p50Ms", "<f8"), ("p99Ms", "<f8"),
                          ("p999Ms", "<f8"), ("maxMs", "<f8"), ("elapsedS", "<f8"), ("imagesPerS", "<f8"),
                          ("peakAdmittedBytes", "<i8"), ("deviceBytes", "<i8")])
-PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "compaction")
-HOST_PHASES = ("plan_upload", "wait", "sort_group")
+PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "grouping", "output")
+HOST_PHASES = ("plan_upload", "wait", "post")
 
-assert DETECT_STATS.itemsize == 152 and DETECT_CONFIG.itemsize == 24
+assert DETECT_STATS.itemsize == 160 and DETECT_CONFIG.itemsize == 24
 assert SERVER_CONFIG.itemsize == 64 and SERVER_STATS.itemsize == 112
 assert HAAR_FEATURE.itemsize == 64 and STUMP4.itemsize == 16 and STAGE.itemsize == 12
 assert DETECTION.itemsize == 24 and TILE_BEST.itemsize == 16 and WEAK.itemsize == 28

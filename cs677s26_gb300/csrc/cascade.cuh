@@ -10,6 +10,7 @@
 // results equal the reference CPU path bit for bit.
 #pragma once
 
+#include "group_dev.cuh"
 #include "integral_dev.cuh"
 
 namespace vjgb {
@@ -98,10 +99,19 @@ struct CtrlHead {
     unsigned long long work[kQueues + 2];  // dynamic work counters of the passes
     unsigned long long stats[4];           // [0] gated windows, [1] stump evaluations
     int qcount[kQueues];                   // entries pushed to queue k (keeps counting past qcap)
-    int compactTotal;                      // raw detections copied to the host buffer
+    int compactTotal;                      // raw detections kept (copied to the host buffer, or grouped)
     int compactOverflow;
+    int rawTotal;                          // raw detections held on the device
+    int grpOverflow;                       // the grouping arrays have fewer slots than compactTotal
+    int grpError;                          // a union-find retry bound ran out
+    int pad;
     // followed by int counts[imageCap] (raw detections per image, counting
-    // past detCap) and int offsets[imageCap] (start in the host buffer)
+    // past detCap), int offsets[imageCap] (start of image i's kept raw
+    // detections, in the host buffer and in the grouping slots), int
+    // rawOff[imageCap] (start of image i's raw detections in flat order), int
+    // ccount[imageCap] (clusters of image i), int gcount[imageCap] (grouped
+    // detections of image i) and uint64 selKey[imageCap] (largest canonical key
+    // kept of image i)
 };
 
 // Everything the persistent kernel reads: written by the host into pinned
@@ -133,7 +143,12 @@ struct DevPlan {
     CtrlHead* ctrl;
     int* counts;                // in the control block
     int* offsets;               // in the control block
+    int* rawOff;                // in the control block
+    int* ccount;                // in the control block
+    int* gcount;                // in the control block
+    unsigned long long* selKey; // in the control block
     vj_detection* hostDets;     // host-mapped, hostCap entries
+    GroupPlan grp;
 };
 
 // ---------------------------------------------------------------------------
@@ -721,6 +736,216 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
 }
 
 // ---------------------------------------------------------------------------
+// Grouping phases (groupRectangles on the device, see group_dev.cuh), between
+// the layout barrier and the output: x histogram, x-order slots, similar
+// pairs and unions, cluster sums, best member, clusters, containment and
+// cluster order.  Returns 0 when a grid barrier failed, 2 when the grouping
+// stopped on an error flag (the host fails the call), 1 when it finished.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned char* dsmem_ptr() {
+    extern __shared__ __align__(16) unsigned char dsmem[];
+    return dsmem;
+}
+
+__device__ __noinline__ int group_phases(const DevPlan& P, GridSync* G, unsigned& epoch, unsigned long long tmo,
+                                          int64_t gtid, int64_t gthreads, int64_t gw, int64_t nw, int lane) {
+    const GroupPlan& GP = P.grp;
+    CtrlHead* C = P.ctrl;
+    const int rawTotal = ld_volatile(&C->rawTotal);
+    const int keptTotal = ld_volatile(&C->compactTotal);
+    auto detAt = [&](int64_t t, int& img) {
+        img = image_of(P.rawOff, P.nImg, t);
+        return ldl2_det(P.dets + static_cast<size_t>(img) * P.detCap + static_cast<size_t>(t - ldl2(P.rawOff + img)));
+    };
+    auto keptOf = [&](int img) { return min(min(ldl2(P.counts + img), P.detCap), GP.limit); };
+
+    // a. x histogram of each image's kept detections
+    for (int64_t t = gtid; t < rawTotal; t += gthreads) {
+        int i;
+        const vj_detection d = detAt(t, i);
+        if (d.x < 0 || d.x >= GP.histBase[i + 1] - GP.histBase[i]) {
+            atomicExch(&C->grpError, 1);  // outside the image: cannot happen for level windows
+            continue;
+        }
+        if (det_key(d) <= ldl2(P.selKey + i)) atomicAdd(GP.hist + GP.histBase[i] + d.x, 1);
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+    if (ld_volatile(&C->grpError) != 0) return 2;
+
+    // b. per image, exclusive scan of the histogram into slot cursors: a
+    // block per image, each thread over a contiguous run of bins
+    {
+        int* wsum = reinterpret_cast<int*>(dsmem_ptr());
+        const int wib = threadIdx.x >> 5;
+        for (int i = blockIdx.x; i < P.nImg; i += gridDim.x) {
+            int* h = GP.hist + GP.histBase[i];
+            const int nb = static_cast<int>(GP.histBase[i + 1] - GP.histBase[i]);
+            const int per = (nb + kCasThreads - 1) / kCasThreads;
+            const int b0 = min(nb, static_cast<int>(threadIdx.x) * per), b1 = min(nb, b0 + per);
+            int sum = 0;
+            for (int b = b0; b < b1; ++b) sum += ldl2(h + b);
+            int inc = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += u;
+            }
+            if (lane == 31) wsum[wib] = inc;
+            __syncthreads();
+            if (wib == 0) {
+                const int v = lane < kCasWarps ? wsum[lane] : 0;
+                int wi = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int u = __shfl_up_sync(0xffffffffu, wi, o);
+                    if (lane >= o) wi += u;
+                }
+                if (lane < kCasWarps) wsum[lane] = wi - v;
+            }
+            __syncthreads();
+            int run = ldl2(P.offsets + i) + wsum[wib] + inc - sum;
+            for (int b = b0; b < b1; ++b) {
+                const int v = ldl2(h + b);
+                h[b] = run;
+                run += v;
+            }
+            __syncthreads();
+        }
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+
+    // c. kept detections into x order (the order among equal x is free: the
+    // pair search below covers every pair within the x reach either way)
+    for (int64_t t = gtid; t < rawTotal; t += gthreads) {
+        int i;
+        const vj_detection d = detAt(t, i);
+        const unsigned long long key = det_key(d);
+        if (key > ldl2(P.selKey + i) || d.x < 0 || d.x >= GP.histBase[i + 1] - GP.histBase[i]) continue;
+        const int sl = atomicAdd(GP.hist + GP.histBase[i] + d.x, 1);
+        GP.x[sl] = d.x;
+        GP.y[sl] = d.y;
+        GP.w[sl] = d.w;
+        GP.h[sl] = d.h;
+        GP.score[sl] = d.score;
+        GP.key[sl] = key;
+        GP.parent[sl] = sl;
+        GP.image[sl] = i;
+        GP.cnt[sl] = 0;
+        GP.best[sl] = 0u;
+        GP.sumX[sl] = 0ull;
+        GP.sumY[sl] = 0ull;
+        GP.sumW[sl] = 0ull;
+        GP.sumH[sl] = 0ull;
+        GP.bestKey[sl] = ~0ull;
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+
+    // d. similar pairs (similarRects, face_vision_engine.cu:585-616) within
+    // the x reach of the earlier rectangle, joined as found: a warp per
+    // rectangle, its lanes over the later rectangles 32 at a time (x order
+    // ends the scan at the first chunk that reaches past the reach)
+    for (int64_t p = gw; p < keptTotal; p += nw) {
+        const int i = ldl2(GP.image + p);
+        const int end = ldl2(P.offsets + i) + keptOf(i);
+        const int ax = ldl2(GP.x + p), ay = ldl2(GP.y + p), aw = ldl2(GP.w + p), ah = ldl2(GP.h + p);
+        const int reach = __float2int_rz(__fmul_rn(__fmul_rn(GP.eps, static_cast<float>(aw + ah)), 0.5f));
+        for (int q0 = static_cast<int>(p) + 1; q0 < end; q0 += 32) {
+            const int q = q0 + lane;
+            bool past = true, sim = false;
+            if (q < end) {
+                const int bx = ldl2(GP.x + q);
+                past = bx > ax + reach;
+                const int by = ldl2(GP.y + q);
+                if (!past && abs(ay - by) <= reach) {
+                    const int bw = ldl2(GP.w + q), bh = ldl2(GP.h + q);
+                    const int delta = __float2int_rz(
+                        __fmul_rn(__fmul_rn(GP.eps, static_cast<float>(min(aw, bw) + min(ah, bh))), 0.5f));
+                    sim = abs(ax - bx) <= delta && abs(ay - by) <= delta && abs(ax + aw - bx - bw) <= delta &&
+                          abs(ay + ah - by - bh) <= delta;
+                }
+            }
+            if (sim && !gf_unite(GP.parent, GP.key, static_cast<int>(p), q)) atomicExch(&C->grpError, 1);
+            if (__any_sync(0xffffffffu, past)) break;
+        }
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+
+    // e. roots, sizes, sums and the largest score of each cluster (the root
+    // goes to its own array: parent entries can still be rewritten to other
+    // ancestors by concurrent finds)
+    for (int64_t p = gtid; p < keptTotal; p += gthreads) {
+        const int r = gf_find(GP.parent, static_cast<int>(p));
+        GP.root[p] = r;
+        atomicAdd(GP.cnt + r, 1);
+        atomicAdd(GP.sumX + r, static_cast<unsigned long long>(ldl2(GP.x + p)));
+        atomicAdd(GP.sumY + r, static_cast<unsigned long long>(ldl2(GP.y + p)));
+        atomicAdd(GP.sumW + r, static_cast<unsigned long long>(ldl2(GP.w + p)));
+        atomicAdd(GP.sumH + r, static_cast<unsigned long long>(ldl2(GP.h + p)));
+        atomicMax(GP.best + r, score_order(ldl2(GP.score + p)));
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+
+    // f. the first member (canonical order) among those with the largest score
+    for (int64_t p = gtid; p < keptTotal; p += gthreads) {
+        const int r = ldl2(GP.root + p);
+        if (score_order(ldl2(GP.score + p)) == ldl2(GP.best + r)) atomicMin(GP.bestKey + r, ldl2(GP.key + p));
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+
+    // g. clusters with more than minN members, written by their best member
+    for (int64_t p = gtid; p < keptTotal; p += gthreads) {
+        const int r = ldl2(GP.root + p);
+        const int n = ldl2(GP.cnt + r);
+        const unsigned long long key = ldl2(GP.key + p);
+        if (key != ldl2(GP.bestKey + r) || n <= GP.minN) continue;
+        const int i = ldl2(GP.image + p);
+        const int c = atomicAdd(P.ccount + i, 1);
+        GCluster g;
+        const unsigned long long un = static_cast<unsigned long long>(n);
+        g.x = static_cast<int>(ldl2(GP.sumX + r) / un);
+        g.y = static_cast<int>(ldl2(GP.sumY + r) / un);
+        g.w = static_cast<int>(ldl2(GP.sumW + r) / un);
+        g.h = static_cast<int>(ldl2(GP.sumH + r) / un);
+        g.n = n;
+        g.scaleIdx = static_cast<int>(key >> 32);
+        g.score = ldl2(GP.score + p);
+        g.image = i;
+        g.key = ldl2(GP.key + r);
+        GP.cl[ldl2(P.offsets + i) + c] = g;
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+
+    // h. containment filter against every other cluster of the image, and
+    // each cluster's rank by first-member key: a warp per cluster
+    for (int64_t p = gw; p < keptTotal; p += nw) {
+        const int i = ldl2(GP.image + p);
+        const int off = ldl2(P.offsets + i);
+        const int k = static_cast<int>(p) - off;
+        const int cc = ldl2(P.ccount + i);
+        if (k >= cc) continue;
+        const GCluster a = ldl2_cluster(GP.cl + p);
+        int rank = 0;
+        bool drop = false;
+        for (int j = lane; j < cc; j += 32) {
+            const GCluster b = ldl2_cluster(GP.cl + off + j);
+            rank += b.key < a.key ? 1 : 0;
+            if (j == k) continue;
+            const int dx = __float2int_rz(__fmul_rn(static_cast<float>(b.w), GP.eps));
+            const int dy = __float2int_rz(__fmul_rn(static_cast<float>(b.h), GP.eps));
+            if (a.x >= b.x - dx && a.y >= b.y - dy && a.x + a.w <= b.x + b.w + dx && a.y + a.h <= b.y + b.h + dy &&
+                (b.n > max(3, a.n) || a.n < 3))
+                drop = true;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rank += __shfl_xor_sync(0xffffffffu, rank, o);
+        drop = __any_sync(0xffffffffu, drop);
+        if (lane == 0) GP.order[off + rank] = drop ? -1 - k : k;
+    }
+    if (!grid_barrier(G, epoch, tmo)) return 0;
+    return ld_volatile(&C->grpError) != 0 ? 2 : 1;
+}
+
+// ---------------------------------------------------------------------------
 // The persistent detection kernel: every phase of a batch in one cooperative
 // launch, phases separated by grid barriers.
 //   1. pyramid: resize chain positions 0, 1, ... (level k from level k-1);
@@ -747,6 +972,10 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     const unsigned long long tmo = P.barrierTimeoutNs ? P.barrierTimeoutNs : kBarrierTimeoutNs;
     if (stamper) G->stamp[0] = global_ns();
     if (P.holdBlock >= 0 && blockIdx.x == static_cast<unsigned>(P.holdBlock)) return;
+    const int64_t gtid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t gthreads = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    if (P.grp.enabled)
+        for (int64_t t = gtid; t < P.grp.histTotal; t += gthreads) P.grp.hist[t] = 0;
 
     // 1. pyramid
     for (int p = 0; p < P.nResize; ++p) {
@@ -806,44 +1035,106 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     if (!grid_barrier(G, epoch, tmo)) return;
     if (stamper) G->stamp[5] = global_ns();
 
-    // 6. compaction: block 0 lays out the images' raw detections in the host
-    // buffer, then every warp copies 32-record chunks.
+    // 6. layout: block 0 places each image's kept raw detections (offsets:
+    // min(count, detCap), and with grouping at most `limit` of them) and its
+    // raw detections in flat order (rawOff); with grouping every block then
+    // finds the truncation key of its images.
+    const GroupPlan& GP = P.grp;
+    const bool grp = GP.enabled != 0;
     if (blockIdx.x == 0) {
-        __shared__ int part[kCasThreads];
+        int* part = reinterpret_cast<int*>(dsmem);
         const int n = P.nImg;
         const int per = (n + kCasThreads - 1) / kCasThreads;
-        const int i0 = threadIdx.x * per, i1 = min(n, i0 + per);
-        int s = 0;
-        for (int i = i0; i < i1; ++i) s += min(P.counts[i], P.detCap);
+        const int i0 = min(n, static_cast<int>(threadIdx.x) * per), i1 = min(n, i0 + per);
+        int s = 0, sr = 0;
+        for (int i = i0; i < i1; ++i) {
+            const int raw = min(ldl2(P.counts + i), P.detCap);
+            sr += raw;
+            s += grp ? min(raw, GP.limit) : raw;
+        }
         part[threadIdx.x] = s;
+        part[kCasThreads + threadIdx.x] = sr;
         __syncthreads();
         if (threadIdx.x == 0) {
-            int run = 0;
+            int run = 0, runr = 0;
             for (int k = 0; k < kCasThreads; ++k) {
-                const int v = part[k];
+                const int v = part[k], vr = part[kCasThreads + k];
                 part[k] = run;
+                part[kCasThreads + k] = runr;
                 run += v;
+                runr += vr;
             }
             C->compactTotal = run;
             C->compactOverflow = run > P.hostCap ? 1 : 0;
+            C->rawTotal = runr;
+            C->grpOverflow = grp && run > GP.cap ? 1 : 0;
         }
         __syncthreads();
-        int off = part[threadIdx.x];
+        int off = part[threadIdx.x], offr = part[kCasThreads + threadIdx.x];
         for (int i = i0; i < i1; ++i) {
+            const int raw = min(ldl2(P.counts + i), P.detCap);
             P.offsets[i] = off;
-            off += min(P.counts[i], P.detCap);
+            P.rawOff[i] = offr;
+            off += grp ? min(raw, GP.limit) : raw;
+            offr += raw;
         }
+        __syncthreads();
     }
-    if (!grid_barrier(G, epoch, tmo)) return;
-    if (C->compactOverflow == 0) {
-        for (int64_t i = gw; i < P.nImg; i += nw) {
-            const int cnt = min(P.counts[i], P.detCap);
-            const int off = P.offsets[i];
-            const vj_detection* src = P.dets + static_cast<size_t>(i) * P.detCap;
-            for (int k = lane; k < cnt; k += 32) P.hostDets[off + k] = src[k];
+    if (grp)
+        for (int i = blockIdx.x; i < P.nImg; i += gridDim.x) {
+            const int raw = min(ldl2(P.counts + i), P.detCap);
+            if (raw > GP.limit) {
+                const unsigned long long k = block_select_key(P.dets + static_cast<size_t>(i) * P.detCap, raw,
+                                                              GP.limit, reinterpret_cast<unsigned*>(dsmem));
+                if (threadIdx.x == 0) P.selKey[i] = k;
+            } else if (threadIdx.x == 0) {
+                P.selKey[i] = ~0ull;
+            }
         }
+    if (!grid_barrier(G, epoch, tmo)) return;
+    bool doGroup = grp && ld_volatile(&C->grpOverflow) == 0 && ld_volatile(&C->compactOverflow) == 0;
+    if (doGroup) {
+        const int r = group_phases(P, G, epoch, tmo, gtid, gthreads, gw, nw, lane);
+        if (r == 0) return;
+        doGroup = r == 1;
     }
     if (stamper) G->stamp[6] = global_ns();
+
+    // 7. output into the host-mapped buffer: the grouped detections of each
+    // image in cluster order, or its raw detections.
+    if (doGroup) {
+        for (int64_t i = gw; i < P.nImg; i += nw) {
+            const int off = ldl2(P.offsets + i), cc = ldl2(P.ccount + i);
+            int outN = 0;
+            for (int b = 0; b < cc; b += 32) {
+                const int k = b + lane;
+                const int v = k < cc ? ldl2(GP.order + off + k) : -1;
+                const bool keep = v >= 0;
+                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const GCluster c = ldl2_cluster(GP.cl + off + v);
+                    vj_detection d;
+                    d.x = c.x;
+                    d.y = c.y;
+                    d.w = c.w;
+                    d.h = c.h;
+                    d.scaleIdx = c.scaleIdx;
+                    d.score = c.score;
+                    P.hostDets[off + outN + __popc(m & lanemask_lt())] = d;
+                }
+                outN += __popc(m);
+            }
+            if (lane == 0) P.gcount[i] = outN;
+        }
+    } else if (!grp && C->compactOverflow == 0) {
+        for (int64_t i = gw; i < P.nImg; i += nw) {
+            const int cnt = min(ldl2(P.counts + i), P.detCap);
+            const int off = ldl2(P.offsets + i);
+            const vj_detection* src = P.dets + static_cast<size_t>(i) * P.detCap;
+            for (int k = lane; k < cnt; k += 32) P.hostDets[off + k] = ldl2_det(src + k);
+        }
+    }
+    if (stamper) G->stamp[7] = global_ns();
 }
 
 }  // namespace vjgb

@@ -172,7 +172,7 @@ struct vj_detector {
     std::vector<DStage> hStages;
     DBuf stumps, pstumps, stages;  // pstumps: planes A, B, C of nStumps uint4 each
     // Work buffers, grown on demand.
-    DBuf imgs, pix, iiSum, iiSq, totS, totQ, qA, qB, dets, dplan, dctrl;
+    DBuf imgs, pix, iiSum, iiSq, totS, totQ, qA, qB, dets, dplan, dctrl, ghist;
     HBuf hplan, hctrl, hdets;
     int imageCap = 0;  // images the control block has room for
     // Optional arena (vj_detector_reserve): every work buffer of a batch is a
@@ -198,6 +198,7 @@ struct vj_detector {
     int64_t qHint = 0;
     int detHint = 0;
     int64_t hostHint = 0;
+    int64_t grpHint = 0;  // kept raw detections of a grouped call
     vj_detect_stats stats{};
     // Wait test (vj_detector_test_barrier_timeout): one block leaves before
     // the first grid barrier and the others wait at most this long.
@@ -270,8 +271,51 @@ size_t smem_bytes(const vj_detector* d, int th) {
     return std::max(lists, deep);
 }
 
-size_t ctrl_bytes(int imageCap) {
-    return align_up(sizeof(CtrlHead), 16) + 2 * sizeof(int) * static_cast<size_t>(imageCap);
+// Control block: CtrlHead, then int counts, offsets, rawOff, ccount and
+// gcount[imageCap], then uint64 selKey[imageCap].
+constexpr int kCtrlIntArrays = 5;
+size_t ctrl_sel_offset(int imageCap) {
+    return align_up(align_up(sizeof(CtrlHead), 16) + kCtrlIntArrays * sizeof(int) * static_cast<size_t>(imageCap), 16);
+}
+size_t ctrl_bytes(int imageCap) { return ctrl_sel_offset(imageCap) + sizeof(uint64_t) * static_cast<size_t>(imageCap); }
+
+// Grouping slots the two queue buffers hold (group_dev.cuh: kGroupBytesA/B
+// per slot, plus alignment).
+int64_t group_slots(size_t qaBytes, size_t qbBytes) {
+    const int64_t a = (static_cast<int64_t>(qaBytes) - 16 * 256) / kGroupBytesA;
+    const int64_t b = (static_cast<int64_t>(qbBytes) - 16 * 256) / kGroupBytesB;
+    return std::max<int64_t>(0, std::min<int64_t>({a, b, INT32_MAX / 2}));
+}
+
+// Carves the grouping arrays of `cap` slots from the queue buffers.
+void carve_group(GroupPlan& g, char* qa, char* qb, int cap) {
+    size_t o = 0;
+    auto take = [&o](char* base, size_t bytes) {
+        o = static_cast<size_t>(align_up(static_cast<int64_t>(o), 256));
+        char* p = base + o;
+        o += bytes;
+        return p;
+    };
+    const size_t n = static_cast<size_t>(cap);
+    g.key = reinterpret_cast<unsigned long long*>(take(qa, 8 * n));
+    g.x = reinterpret_cast<int*>(take(qa, 4 * n));
+    g.y = reinterpret_cast<int*>(take(qa, 4 * n));
+    g.w = reinterpret_cast<int*>(take(qa, 4 * n));
+    g.h = reinterpret_cast<int*>(take(qa, 4 * n));
+    g.score = reinterpret_cast<float*>(take(qa, 4 * n));
+    g.parent = reinterpret_cast<int*>(take(qa, 4 * n));
+    g.root = reinterpret_cast<int*>(take(qa, 4 * n));
+    g.image = reinterpret_cast<int*>(take(qa, 4 * n));
+    o = 0;
+    g.sumX = reinterpret_cast<unsigned long long*>(take(qb, 8 * n));
+    g.sumY = reinterpret_cast<unsigned long long*>(take(qb, 8 * n));
+    g.sumW = reinterpret_cast<unsigned long long*>(take(qb, 8 * n));
+    g.sumH = reinterpret_cast<unsigned long long*>(take(qb, 8 * n));
+    g.bestKey = reinterpret_cast<unsigned long long*>(take(qb, 8 * n));
+    g.cl = reinterpret_cast<GCluster*>(take(qb, sizeof(GCluster) * n));
+    g.cnt = reinterpret_cast<int*>(take(qb, 4 * n));
+    g.best = reinterpret_cast<unsigned*>(take(qb, 4 * n));
+    g.order = reinterpret_cast<int*>(take(qb, 4 * n));
 }
 
 // Builds (or rebuilds) the launch graph for the current launch shape and
@@ -350,10 +394,21 @@ struct BatchImage {
     int64_t stride;
 };
 
-// Runs the detection kernel over `ims`; on return the raw detections of image
-// i are hdets[offsets[i] .. offsets[i] + min(counts[i], detCap)).
+// Grouping on the device: off, or on with groupRectangles' minNeighbors and
+// the per-image raw detection limit.
+struct GroupArgs {
+    bool on = false;
+    int minN = 0;
+    int limit = 0;
+};
+
+// Runs the detection kernel over `ims`.  On return, without grouping, the raw
+// detections of image i are hdets[offsets[i] .. offsets[i] + min(counts[i],
+// detCap)); with grouping its grouped detections are hdets[offsets[i] ..
+// offsets[i] + grouped[i]) in cluster order.
 int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, float sf, int minObj,
-            cudaStream_t s, const int** outCounts, const int** outOffsets, int* outDetCap) {
+            const GroupArgs& ga, cudaStream_t s, const int** outCounts, const int** outOffsets, int* outDetCap,
+            const int** outGrouped = nullptr) {
     const int nImg = static_cast<int>(ims.size());
     const double t0 = now_ms();
     // ---- levels and sizes
@@ -379,7 +434,13 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             windowsAll += static_cast<int64_t>((g.w - D->winW + g.step) / g.step) * ((g.h - D->winH + g.step) / g.step);
         }
     const int64_t totElems = std::max<int64_t>(1, totRows * totPitch);
-    int64_t qcap = std::min<int64_t>(std::max<int64_t>({windowsAll / 8, int64_t(1) << 16, D->qHint}), INT32_MAX / 2);
+    // the grouping arrays reuse the queue buffers after the deep pass
+    const int64_t grpQ = ga.on ? (D->grpHint * kGroupBytesB + 16 * 256) / static_cast<int64_t>(sizeof(QEntry)) + 1 : 0;
+    int64_t qcap =
+        std::min<int64_t>(std::max<int64_t>({windowsAll / 8, int64_t(1) << 16, D->qHint, grpQ}), INT32_MAX / 2);
+    std::vector<int64_t> histBase(static_cast<size_t>(nImg) + 1, 0);
+    for (int i = 0; i < nImg; ++i) histBase[i + 1] = histBase[i] + ims[i].w + 1;
+    const int64_t histTotal = ga.on ? histBase[nImg] : 0;
     int detCap = std::max({64, std::min(D->maxDet, 4096), D->detHint});
     // Work buffers: grown on demand, or carved from the arena with the queues
     // taking whatever the other buffers leave.
@@ -394,6 +455,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             if ((r = D->totS.ensure(totElems * 4)) != VJ_OK) return r;
             if ((r = D->totQ.ensure(totElems * 8)) != VJ_OK) return r;
             if ((r = D->dets.ensure(detBytes)) != VJ_OK) return r;
+            if (histTotal && (r = D->ghist.ensure(static_cast<size_t>(histTotal) * 4)) != VJ_OK) return r;
             if ((r = D->qA.ensure(sizeof(QEntry) * static_cast<size_t>(qcap))) != VJ_OK) return r;
             return D->qB.ensure(sizeof(QEntry) * static_cast<size_t>(qcap));
         }
@@ -418,10 +480,11 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         carve(D->totS, static_cast<size_t>(totElems) * 4);
         carve(D->totQ, static_cast<size_t>(totElems) * 8);
         carve(D->dets, detBytes);
+        if (histTotal) carve(D->ghist, static_cast<size_t>(histTotal) * 4);
         off = static_cast<size_t>(align_up(static_cast<int64_t>(off), 256));
         const int64_t room = fits && off < cap ? static_cast<int64_t>((cap - off) / 2 / sizeof(QEntry)) - 32 : 0;
         const int64_t q = std::min<int64_t>(room, INT32_MAX / 2);
-        if (!fits || q < std::max<int64_t>(windowsAll / 8, 1))
+        if (!fits || q < std::max<int64_t>({windowsAll / 8, grpQ, 1}))
             return set_error(VJ_OUT_OF_MEMORY, "detector arena: " + std::to_string(cap) +
                                                    " reserved bytes do not hold this batch");
         qcap = q;
@@ -524,7 +587,8 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     const int64_t oRj = align_up(oItems + sizeof(int64_t) * rjItems.size(), 64);
     const int64_t oII = align_up(oRj + sizeof(ResizeJob) * std::max<size_t>(rjAll.size(), 1), 64);
     const int64_t oLv = align_up(oII + sizeof(IIJob) * std::max<size_t>(iij.size(), 1), 64);
-    const int64_t planBytes = align_up(oLv + sizeof(CasLevel) * std::max<size_t>(lv.size(), 1), 64);
+    const int64_t oHist = align_up(oLv + sizeof(CasLevel) * std::max<size_t>(lv.size(), 1), 64);
+    const int64_t planBytes = align_up(oHist + sizeof(int64_t) * histBase.size(), 64);
     if (planBytes > static_cast<int64_t>(D->dplan.cap) || planBytes > static_cast<int64_t>(D->hplan.cap)) {
         const int64_t want = std::max<int64_t>(planBytes, 1 << 20);
         if ((st = D->dplan.ensure(want)) != VJ_OK) return st;
@@ -542,6 +606,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     if (!rjAll.empty()) std::memcpy(hp + oRj, rjAll.data(), sizeof(ResizeJob) * rjAll.size());
     std::memcpy(hp + oII, iij.data(), sizeof(IIJob) * iij.size());
     std::memcpy(hp + oLv, lv.data(), sizeof(CasLevel) * lv.size());
+    std::memcpy(hp + oHist, histBase.data(), sizeof(int64_t) * histBase.size());
 
     vj_detect_stats& S = D->stats;
     S = vj_detect_stats{};
@@ -596,7 +661,23 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         P.ctrl = D->dctrl.as<CtrlHead>();
         P.counts = reinterpret_cast<int*>(D->dctrl.as<char>() + align_up(sizeof(CtrlHead), 16));
         P.offsets = P.counts + D->imageCap;
+        P.rawOff = P.offsets + D->imageCap;
+        P.ccount = P.rawOff + D->imageCap;
+        P.gcount = P.ccount + D->imageCap;
+        P.selKey = reinterpret_cast<unsigned long long*>(D->dctrl.as<char>() + ctrl_sel_offset(D->imageCap));
         P.hostDets = static_cast<vj_detection*>(D->hdets.dev);
+        if (ga.on) {
+            GroupPlan& g = P.grp;
+            g.enabled = 1;
+            g.minN = std::max(1, ga.minN);
+            g.limit = std::max(1, ga.limit);
+            g.cap = static_cast<int>(group_slots(D->qA.cap, D->qB.cap));
+            g.eps = 0.2f;
+            g.histBase = reinterpret_cast<const int64_t*>(dp + oHist);
+            g.hist = D->ghist.as<int>();
+            g.histTotal = histTotal;
+            carve_group(g, D->qA.as<char>(), D->qB.as<char>(), g.cap);
+        }
         std::memcpy(hp, &P, sizeof(P));
         if ((st = ensure_graph(D, static_cast<size_t>(planBytes))) != VJ_OK) return st;
         VJ_CUDA_TRY(cudaGraphExecMemcpyNodeSetParams1D(D->exec, D->planNode, D->dplan.p, D->hplan.p,
@@ -618,6 +699,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         VJ_CUDA_TRY(cudaEventElapsedTime(&ms, D->ev0, D->ev1));
         const CtrlHead* H = D->hctrl.as<CtrlHead>();
         if (H->sync.error) return set_error(VJ_RUNTIME_ERROR, "detection kernel: a grid barrier wait timed out");
+        if (ga.on && H->grpError) return set_error(VJ_RUNTIME_ERROR, "detection kernel: grouping stopped on an error");
         const int* hc = reinterpret_cast<const int*>(D->hctrl.as<char>() + align_up(sizeof(CtrlHead), 16));
         int need = 0, qneed = 0;
         int64_t total = 0;
@@ -630,8 +712,10 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         D->detHint = std::max(D->detHint, need + need / 4);
         D->hostHint = std::max<int64_t>(D->hostHint, total + total / 4);
         S.attempts = attempt + 1;
-        if (qneed > qcap || need > detCap || H->compactOverflow) {
-            qcap = std::min<int64_t>(std::max<int64_t>(qcap, qneed + qneed / 4), INT32_MAX / 2);
+        if (ga.on) D->grpHint = std::max<int64_t>(D->grpHint, H->compactTotal + H->compactTotal / 4);
+        if (qneed > qcap || need > detCap || H->compactOverflow || (ga.on && H->grpOverflow)) {
+            const int64_t gq = ga.on ? (D->grpHint * kGroupBytesB + 16 * 256) / static_cast<int64_t>(sizeof(QEntry)) + 1 : 0;
+            qcap = std::min<int64_t>(std::max<int64_t>({qcap, qneed + qneed / 4, gq}), INT32_MAX / 2);
             detCap = std::max(detCap, need + need / 4);
             hostCap = std::max<int64_t>(hostCap, total + total / 4);
             continue;
@@ -643,13 +727,14 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         S.stumpEvals = static_cast<int64_t>(H->stats[1]);
         S.rawDetections = H->compactTotal;
         S.deepWindows = D->deepFrom < D->nStages ? H->qcount[D->queueEnds.size()] : 0;
-        for (int k = 0; k < 6; ++k) {
+        for (int k = 0; k < kPhaseStamps - 1; ++k) {
             const unsigned long long a = H->sync.stamp[k], b = H->sync.stamp[k + 1];
             S.phaseMs[k] = (a && b >= a) ? static_cast<double>(b - a) * 1e-6 : 0.0;
         }
         *outCounts = hc;
         *outOffsets = hc + D->imageCap;
         *outDetCap = detCap;
+        if (outGrouped) *outGrouped = hc + 4 * D->imageCap;
         return VJ_OK;
     }
     return set_error(VJ_RUNTIME_ERROR, "detection buffers still overflow after growing them");
@@ -659,24 +744,37 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
               int maxDet, bool group, vj_detection* out, int capPer, int* counts, cudaStream_t s) {
     const int* hc = nullptr;
     const int* ho = nullptr;
+    const int* hg = nullptr;
     int detCap = 0;
-    const int st = execute(D, ims, onDevice, sf, minObj, s, &hc, &ho, &detCap);
+    GroupArgs ga;
+    ga.on = group;
+    ga.minN = minN;
+    ga.limit = std::max(1, maxDet);
+    const int st = execute(D, ims, onDevice, sf, minObj, ga, s, &hc, &ho, &detCap, &hg);
     if (st != VJ_OK) return st;
     const double t0 = now_ms();
     const int nImg = static_cast<int>(ims.size());
+    if (group) {
+        // grouped on the device: copy each image's clusters out
+        const vj_detection* hd = D->hdets.as<vj_detection>();
+        for (int i = 0; i < nImg; ++i) {
+            const int k = std::min(hg[i], capPer);
+            if (k > 0) std::memcpy(out + static_cast<size_t>(i) * capPer, hd + ho[i], sizeof(vj_detection) * k);
+            counts[i] = k;
+        }
+        D->stats.hostMs[2] = now_ms() - t0;
+        return VJ_OK;
+    }
     const int limit = std::max(1, maxDet);
     const vj_detection* hd = D->hdets.as<vj_detection>();
-    const int hw = std::max(1, static_cast<int>(std::thread::hardware_concurrency()));
-    // batches post-process images in parallel; a few images use the threads inside grouping
-    const int groupThreads = nImg >= 8 ? 1 : std::min(8, hw);
+    // raw detections: canonical order, the first maxDet of each image
     auto post = [&](int i) {
         const vj_detection* src = hd + ho[i];
         std::vector<vj_detection> raw(src, src + std::min(hc[i], detCap));
         canonical_sort(raw);
         if (static_cast<int>(raw.size()) > limit) raw.resize(limit);
-        std::vector<vj_detection> res = group ? group_rectangles(raw, minN, 0.2f, groupThreads) : std::move(raw);
-        const int k = std::min(static_cast<int>(res.size()), capPer);
-        if (k > 0) std::memcpy(out + static_cast<size_t>(i) * capPer, res.data(), sizeof(vj_detection) * k);
+        const int k = std::min(static_cast<int>(raw.size()), capPer);
+        if (k > 0) std::memcpy(out + static_cast<size_t>(i) * capPer, raw.data(), sizeof(vj_detection) * k);
         counts[i] = k;
     };
     if (nImg >= 8) {
@@ -739,7 +837,7 @@ int vj_detector_destroy(vj_detector* d) {
     if (d->ev0) cudaEventDestroy(d->ev0);
     if (d->ev1) cudaEventDestroy(d->ev1);
     for (DBuf* b : {&d->stumps, &d->pstumps, &d->stages, &d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS, &d->totQ,
-                    &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->arena})
+                    &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->ghist, &d->arena})
         b->release();
     d->hplan.release();
     d->hctrl.release();
@@ -853,7 +951,8 @@ int vj_detector_get_config(const vj_detector* d, vj_detect_config* cfg) {
 
 int vj_detector_reserve(vj_detector* d, int64_t bytes) {
     if (!d || bytes < 0) return set_error(VJ_INVALID_ARG, "vj_detector_reserve: bad arguments");
-    for (DBuf* b : {&d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS, &d->totQ, &d->qA, &d->qB, &d->dets}) b->release();
+    for (DBuf* b : {&d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS, &d->totQ, &d->qA, &d->qB, &d->dets, &d->ghist})
+        b->release();
     d->arena.release();
     if (bytes == 0) return ok();
     const cudaError_t e = cudaMalloc(&d->arena.p, static_cast<size_t>(bytes));
@@ -881,7 +980,7 @@ int vj_detector_device_bytes(const vj_detector* d, int64_t* bytes) {
     if (!d || !bytes) return set_error(VJ_INVALID_ARG, "vj_detector_device_bytes: null argument");
     int64_t t = 0;
     for (const DBuf* b : {&d->stumps, &d->pstumps, &d->stages, &d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS,
-                          &d->totQ, &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->arena})
+                          &d->totQ, &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->ghist, &d->arena})
         if (!b->view) t += static_cast<int64_t>(b->cap);
     *bytes = t;
     return ok();
@@ -891,7 +990,7 @@ int vj_detect_estimate_bytes(int winW, int winH, int w, int h, float scaleFactor
                              int maxDetections, int64_t* bytes) {
     if (!bytes || winW < 3 || winH < 3 || w <= 0 || h <= 0 || !(scaleFactor > 1.0f) || minObjectSize < 1)
         return set_error(VJ_INVALID_ARG, "vj_detect_estimate_bytes: bad arguments");
-    int64_t t = align_up(w, 16) * h;  // image copy
+    int64_t t = align_up(w, 16) * h + 4 * (static_cast<int64_t>(w) + 1);  // image copy, grouping histogram
     for (const LevelGeom& g : plan_levels(w, h, winW, winH, scaleFactor, minObjectSize)) {
         if (g.src != -2) t += align_up(g.w, 16) * g.h;           // resized level
         const int64_t ii = static_cast<int64_t>(g.h + 1) * ii_pitch(g.w);
@@ -995,7 +1094,8 @@ int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images, co
         const int* hc = nullptr;
         const int* ho = nullptr;
         int detCap = 0;
-        int r = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, nullptr, &hc, &ho, &detCap);
+        int r = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, GroupArgs{}, nullptr, &hc, &ho,
+                        &detCap);
         if (r != VJ_OK) return r;
         std::vector<std::vector<vj_detection>> got(static_cast<size_t>(n));
         const vj_detection* hd = d->hdets.as<vj_detection>();
@@ -1015,7 +1115,8 @@ int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images, co
         }
         std::vector<double> t;
         for (int k = 0; k < repeats; ++k) {
-            r = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, nullptr, &hc, &ho, &detCap);
+            r = execute(d, ims, images_on_device != 0, scaleFactor, minObjectSize, GroupArgs{}, nullptr, &hc, &ho,
+                        &detCap);
             if (r != VJ_OK) return r;
             t.push_back(d->stats.gpuMs);
         }

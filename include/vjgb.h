@@ -359,19 +359,24 @@ int vj_detector_set_norm_mode(vj_detector* d, int mode);
 /* FaceVisionEngine::detectMultiScale, face_vision_engine.cu:1541-1747.
  * image is a host pointer unless image_on_device != 0.  Raw detections are
  * returned in canonical order (pyramid level, then y, then x), the order of
- * the reference's CPU path (main.cu:765-818); with applyGrouping the
- * groupRectangles step (eps 0.2, face_vision_engine.cu:1401-1539) runs on that
- * list.  `out` is a host array of `capacity` entries; *count receives the
- * number written.  Blocks until the result is on the host, like the
- * reference. */
+ * the reference's CPU path (main.cu:765-818), the first maxDetections of them.
+ * With applyGrouping the groupRectangles step (eps 0.2,
+ * face_vision_engine.cu:1401-1539) runs on the device over that list: the
+ * clusters, their averages, scores and scaleIdx and the containment filter
+ * are the reference's; the clusters come out ordered by the canonical position
+ * of their first member (the reference's own order follows its raw
+ * detections' atomic order).  `out` is a host array of `capacity` entries;
+ * *count receives the number written.  Blocks until the result is on the
+ * host, like the reference. */
 int vj_detect(vj_detector* d, const uint8_t* image, int w, int h, int stride,
               int image_on_device, float scaleFactor, int minNeighbors,
               int minObjectSize, int maxDetections, int applyGrouping,
               vj_detection* out, int capacity, int* count, void* stream);
 
-/* FaceVisionEngine::groupRectanglesCpu (face_vision_engine.cu:1401-1539), the
- * host step of detectMultiScale with applyGrouping, exposed so raw detections
- * can be grouped separately.  out needs room for n entries. */
+/* FaceVisionEngine::groupRectanglesCpu (face_vision_engine.cu:1401-1539) on
+ * the host, with the reference's cluster order for the given input order,
+ * exposed so raw detections can be grouped separately (vj_detect groups on
+ * the device).  out needs room for n entries. */
 int vj_group_rectangles(const vj_detection* in, int n, int minNeighbors, float eps,
                         vj_detection* out, int* count);
 
@@ -402,10 +407,11 @@ typedef struct vj_detect_stats {
     int32_t attempts;        /* 1, or more when a work buffer had to grow */
     int32_t queuePasses;     /* lane-per-window queue passes after the tile pass */
     double gpuMs;            /* device time of the detection launch */
-    double phaseMs[6];       /* pyramid, integrals, tile pass, queue passes,
-                                deep pass, compaction of the raw detections */
+    double phaseMs[7];       /* pyramid, integrals, tile pass, queue passes,
+                                deep pass, grouping, output to the host buffer */
     double hostMs[3];        /* host wall time: planning and upload, waiting
-                                for the device, sorting and grouping */
+                                for the device, sorting raw detections or
+                                copying grouped ones */
 } vj_detect_stats;
 
 int vj_detector_last_stats(const vj_detector* d, vj_detect_stats* out);

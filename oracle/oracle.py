@@ -69,6 +69,8 @@ def lib() -> C.CDLL:
                                  i32, vp, i32]
         L.vjo_group.restype = i32
         L.vjo_group.argtypes = [vp, i32, i32, f32, vp]
+        L.vjo_group_first_order.restype = i32
+        L.vjo_group_first_order.argtypes = [vp, i32, i32, f32, vp]
         _lib = L
     return _lib
 
@@ -182,4 +184,12 @@ def group(dets, min_neighbors=4, eps=0.2):
     dets = np.ascontiguousarray(dets, dtype=DET)
     out = np.zeros(max(1, len(dets)), dtype=DET)
     n = lib().vjo_group(_p(dets), len(dets), min_neighbors, eps, _p(out))
+    return out[:n].copy()
+
+
+def group_first_order(dets, min_neighbors=4, eps=0.2):
+    """group() with the clusters ordered by their first member's input index."""
+    dets = np.ascontiguousarray(dets, dtype=DET)
+    out = np.zeros(max(1, len(dets)), dtype=DET)
+    n = lib().vjo_group_first_order(_p(dets), len(dets), min_neighbors, eps, _p(out))
     return out[:n].copy()

@@ -768,7 +768,9 @@ static int cmp_x_then_index(const void* pa, const void* pb) {
     return a < b ? -1 : (a > b ? 1 : 0);
 }
 
-int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out) {
+/* groupRectanglesCpu; when `first` is given it receives, per output cluster,
+ * the smallest input index among the cluster's members. */
+static int group_impl(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out, int* first) {
     if (n <= 0) return 0;
     int* p = (int*)malloc(sizeof(int) * (size_t)n);
     int* rk = (int*)calloc((size_t)n, sizeof(int));
@@ -797,9 +799,14 @@ int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* ou
     int* cnt = (int*)calloc((size_t)n, sizeof(int));
     float* bs = (float*)malloc(sizeof(float) * (size_t)n);
     int* bsi = (int*)calloc((size_t)n, sizeof(int));
-    for (int i = 0; i < n; ++i) bs[i] = -INFINITY;
+    int* fst = (int*)malloc(sizeof(int) * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        bs[i] = -INFINITY;
+        fst[i] = -1;
+    }
     for (int i = 0; i < n; ++i) {
         const int r = dsu_find(p, i);
+        if (fst[r] < 0) fst[r] = i;
         sx[r] += in[i].x;
         sy[r] += in[i].y;
         sw[r] += in[i].w;
@@ -812,6 +819,7 @@ int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* ou
     }
     vjo_det* cl = (vjo_det*)malloc(sizeof(vjo_det) * (size_t)n);
     int* cc = (int*)malloc(sizeof(int) * (size_t)n);
+    int* cf = (int*)malloc(sizeof(int) * (size_t)n);
     int m = 0;
     const int minN = minNeighbors > 1 ? minNeighbors : 1;
     for (int i = 0; i < n; ++i) {
@@ -826,6 +834,7 @@ int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* ou
         d.score = bs[i];
         cl[m] = d;
         cc[m] = cnt[i];
+        cf[m] = fst[i];
         ++m;
     }
     int maxW = 0;
@@ -857,7 +866,10 @@ int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* ou
                 break;
             }
         }
-        if (!discard) out[k++] = *r1;
+        if (!discard) {
+            if (first) first[k] = cf[i];
+            out[k++] = *r1;
+        }
     }
     free(p);
     free(rk);
@@ -869,8 +881,40 @@ int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* ou
     free(cnt);
     free(bs);
     free(bsi);
+    free(fst);
     free(cl);
     free(cc);
+    free(cf);
     free(co);
+    return k;
+}
+
+int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out) {
+    return group_impl(in, n, minNeighbors, eps, out, NULL);
+}
+
+/* The same clusters ordered by their first member's input index (the
+ * library's device grouping order when the input is in canonical order). */
+int vjo_group_first_order(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out) {
+    if (n <= 0) return 0;
+    vjo_det* tmp = (vjo_det*)malloc(sizeof(vjo_det) * (size_t)n);
+    int* first = (int*)malloc(sizeof(int) * (size_t)n);
+    const int k = group_impl(in, n, minNeighbors, eps, tmp, first);
+    /* insertion by first index: the first indices are distinct */
+    int* pos = (int*)malloc(sizeof(int) * (size_t)(k > 0 ? k : 1));
+    for (int i = 0; i < k; ++i) pos[i] = i;
+    for (int i = 1; i < k; ++i) {
+        const int v = pos[i];
+        int j = i - 1;
+        while (j >= 0 && first[pos[j]] > first[v]) {
+            pos[j + 1] = pos[j];
+            --j;
+        }
+        pos[j + 1] = v;
+    }
+    for (int i = 0; i < k; ++i) out[i] = tmp[pos[i]];
+    free(tmp);
+    free(first);
+    free(pos);
     return k;
 }

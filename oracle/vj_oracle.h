@@ -109,6 +109,9 @@ int vjo_detect(const vjo_feature* feats, int nFeat, const vjo_stump* stumps, int
 
 /* groupRectanglesCpu, face_vision_engine.cu:1401-1539.  Returns the count. */
 int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out);
+/* vjo_group with the output ordered by each cluster's first member (smallest
+ * input index). */
+int vjo_group_first_order(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out);
 
 #ifdef __cplusplus
 }

@@ -203,3 +203,15 @@ def test_group_rectangles_large_input_matches_oracle(vj, oracle, basic_pool):
         assert lib.vj_group_rectangles(raw.ctypes.data, len(raw), minn, C.c_float(0.2), out.ctypes.data,
                                        C.byref(n)) == 0
         assert out[: n.value].tobytes() == oracle.group(raw, minn, 0.2).tobytes()
+
+
+def test_oracle_first_member_order_is_a_permutation(vj, oracle, basic_pool):
+    """The oracle's first-member ordering (the device grouping's output order)
+    holds the same clusters as its reference-order grouping."""
+    st, sg = vj.synth_cascade(2)
+    scene = vj.synth_scene(7, 800, 600, 12, 24, 200)
+    raw = oracle.detect(basic_pool, st, sg, scene, norm_mode=0, threads=8)
+    for minn in (0, 2, 4):
+        a, b = oracle.group(raw, minn, 0.2), oracle.group_first_order(raw, minn, 0.2)
+        assert len(a) == len(b) > 0
+        assert sorted(x.tobytes() for x in a) == sorted(x.tobytes() for x in b)

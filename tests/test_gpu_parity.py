@@ -230,14 +230,22 @@ def detector(vj, pool, st, sg, w=3840, h=2160, norm=0):
     return e
 
 
-def test_detect_golden(cuda, vj, golden, gin, basic_pool):
+def as_set(dets):
+    """Detections as a sorted list of records (groupRectangles' output order
+    is not part of the reference's contract)."""
+    return sorted(bytes(r) for r in np.ascontiguousarray(dets).view(np.uint8).reshape(-1, 24))
+
+
+def test_detect_golden(cuda, vj, oracle, golden, gin, basic_pool):
     e = detector(vj, basic_pool, gin["det_stumps"], gin["det_stages"], norm=1)
     for g in golden["detect"]:
         scene = gin[f"det_scene_{g['key']}"]
         st, raw = e.detectMultiScale(scene, g["w"], g["h"], g["w"], 1.25, 4, 24, 200000, applyGrouping=False)
         assert st == 0 and raw.tobytes() == gin[f"det_raw_{g['key']}"].tobytes()
         st, grp = e.detectMultiScale(scene, g["w"], g["h"], g["w"], 1.25, 4, 24, 200000, applyGrouping=True)
-        assert st == 0 and grp.tobytes() == gin[f"det_grouped_{g['key']}"].tobytes()
+        # grouped on the device: the reference's clusters, in first-member order
+        assert st == 0 and as_set(grp) == as_set(gin[f"det_grouped_{g['key']}"])
+        assert grp.tobytes() == oracle.group_first_order(raw, 4, 0.2).tobytes()
     st, raw = e.detectMultiScale(gin["det_scene_0"], 320, 240, 320, 1.25, 4, 24, 50, applyGrouping=False)
     assert raw.tobytes() == gin["det_trunc"].tobytes()
 
@@ -251,7 +259,41 @@ def test_detect_1080p_full_cascade(cuda, vj, oracle, basic_pool, norm):
     ref = oracle.detect(basic_pool, st, sg, scene, norm_mode=norm, threads=8)
     assert s == 0 and len(raw) == len(ref) and raw.tobytes() == ref.tobytes()
     s, grp = e.detectMultiScale(scene, 1920, 1080, 1920, 1.25, 4, 24, 200000)
-    assert grp.tobytes() == oracle.group(ref, 4, 0.2).tobytes()
+    assert s == 0 and grp.tobytes() == oracle.group_first_order(ref, 4, 0.2).tobytes()
+    assert as_set(grp) == as_set(oracle.group(ref, 4, 0.2))
+
+
+def test_device_grouping_parameters_and_batches(cuda, vj, oracle, basic_pool):
+    """Device groupRectangles against the oracle's restatement of
+    groupRectanglesCpu over the canonical raw list: every minNeighbors branch
+    (the containment test's n < 3 case included), truncation to
+    maxDetections before grouping, and a batch grouped image by image."""
+    st, sg = vj.synth_cascade(2)
+    e = detector(vj, basic_pool, st, sg)
+    scenes = [vj.synth_scene(1, 1920, 1080, 40, 24, 300), vj.synth_scene(7, 800, 600, 12, 24, 200),
+              vj.synth_scene(9, 333, 251, 3, 24, 120)]
+    raws = []
+    for sc in scenes:
+        h, w = sc.shape
+        s, raw = e.detectMultiScale(sc, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+        assert s == 0
+        raws.append(raw)
+    assert len(raws[0]) > 5000  # dense clusters around the pasted faces
+    for mn in (0, 1, 2, 3, 6):
+        for sc, raw in zip(scenes, raws):
+            h, w = sc.shape
+            s, grp = e.detectMultiScale(sc, w, h, w, 1.25, mn, 24, 200000)
+            assert s == 0 and grp.tobytes() == oracle.group_first_order(raw, mn, 0.2).tobytes(), (mn, w)
+    for lim in (1, 37, 1000):
+        sc, raw = scenes[0], raws[0]
+        s, grp = e.detectMultiScale(sc, 1920, 1080, 1920, 1.25, 2, 24, lim)
+        assert s == 0 and grp.tobytes() == oracle.group_first_order(raw[:lim], 2, 0.2).tobytes(), lim
+    s, outs = e.detectBatch(scenes, minNeighbors=3, capPerImage=20000)
+    assert s == 0
+    for raw, got in zip(raws, outs):
+        assert got.tobytes() == oracle.group_first_order(raw, 3, 0.2).tobytes()
+    k = e.lastStats()
+    assert k["phaseMs"]["grouping"] > 0.0 and k["hostMs"]["post"] < 50.0
 
 
 def test_detect_device_image_and_strides(cuda, vj, oracle, basic_pool, gin):
