@@ -24,6 +24,7 @@
 
 #include "cascade.cuh"
 #include "group.h"
+#include "launch_chain.h"
 
 namespace vjgb {
 namespace {
@@ -204,6 +205,7 @@ struct vj_detector {
     // the first grid barrier and the others wait at most this long.
     int testHoldBlock = -1;
     unsigned long long testBarrierTimeoutNs = 0;
+    LaunchChain* chain = nullptr;  // launch ordering shared with other detectors
 };
 
 namespace {
@@ -686,12 +688,23 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             for (int i = 0; i < nImg; ++i)
                 VJ_CUDA_TRY(cudaMemcpy2DAsync(D->imgs.as<uint8_t>() + imgOff[i], align_up(ims[i].w, 16), ims[i].ptr,
                                               ims[i].stride, ims[i].w, ims[i].h, cudaMemcpyHostToDevice, s));
-        VJ_CUDA_TRY(cudaEventRecord(D->ev0, s));
-        cudaError_t le = cudaSuccess;
-        VJ_TIMED_LAUNCH("detect_persistent_kernel", s, le = cudaGraphLaunch(D->exec, s));
-        if (le != cudaSuccess)
-            return set_error(VJ_CUDA_ERROR, std::string("detection graph launch: ") + cudaGetErrorString(le));
-        VJ_CUDA_TRY(cudaEventRecord(D->ev1, s));
+        {
+            std::unique_lock<std::mutex> chainLock;
+            if (D->chain) {
+                chainLock = std::unique_lock<std::mutex>(D->chain->mu);
+                if (D->chain->last) VJ_CUDA_TRY(cudaStreamWaitEvent(s, D->chain->last, 0));
+            }
+            VJ_CUDA_TRY(cudaEventRecord(D->ev0, s));
+            cudaError_t le = cudaSuccess;
+            VJ_TIMED_LAUNCH("detect_persistent_kernel", s, le = cudaGraphLaunch(D->exec, s));
+            if (le != cudaSuccess)
+                return set_error(VJ_CUDA_ERROR, std::string("detection graph launch: ") + cudaGetErrorString(le));
+            VJ_CUDA_TRY(cudaEventRecord(D->ev1, s));
+            if (D->chain) {
+                if (!D->chain->last) VJ_CUDA_TRY(cudaEventCreateWithFlags(&D->chain->last, cudaEventDisableTiming));
+                VJ_CUDA_TRY(cudaEventRecord(D->chain->last, s));
+            }
+        }
         const double t1 = now_ms();
         VJ_CUDA_TRY(cudaStreamSynchronize(s));
         const double t2 = now_ms();
@@ -812,6 +825,16 @@ int collect_images(vj_detector* d, int n, const uint8_t* const* images, const in
 }
 
 }  // namespace
+
+namespace vjgb {
+
+int detector_set_launch_chain(vj_detector* d, LaunchChain* chain) {
+    if (!d) return set_error(VJ_INVALID_ARG, "detector_set_launch_chain: null detector");
+    d->chain = chain;
+    return ok();
+}
+
+}  // namespace vjgb
 
 extern "C" {
 

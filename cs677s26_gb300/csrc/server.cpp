@@ -4,11 +4,14 @@
 // per worker.  A worker owns a vj_detector and a CUDA stream.  When it is
 // free it takes, in arrival order, every queued request that fits its share
 // of the HBM budget and runs them as one vj_detect_batch launch (one
-// persistent kernel over all their pyramid levels); requests that arrive
-// while batches are on the GPU wait for the next free worker.  Each worker's
-// launches use part of every SM, so the batches of different workers run on
-// the device at the same time, and one worker's host work (planning, upload,
-// sorting and grouping) overlaps another's kernel.
+// persistent kernel over all their pyramid levels, grouping included);
+// requests that arrive while batches are on the GPU wait for the next free
+// worker.  By default every worker's kernel fills the GPU (all resident CTAs
+// per SM) and the kernels follow one another on the device through a shared
+// launch chain, so a lone request gets the whole GPU, while one worker's host
+// work and uploads overlap another's kernel.  A configured blocksPerSM below
+// the full residency instead splits the SMs and lets the workers' kernels
+// run side by side.
 //
 // Request images are copied at submit into pinned host buffers drawn from a
 // pool, so the worker's upload is a DMA from pinned memory and the caller's
@@ -28,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include "common.h"
+#include "launch_chain.h"
 
 namespace vjgb {
 namespace {
@@ -99,6 +103,7 @@ struct vj_server {
     std::vector<cudaStream_t> streams;
     std::vector<std::thread> threads;
     PinnedPool pool;
+    LaunchChain chain;
 
     std::mutex mu;
     std::condition_variable cvWork;  // workers: queue not empty or stopping
@@ -230,8 +235,10 @@ int vj_server_create(const vj_server_config* cfg, const vj_haar_feature* feature
         int fit = 0;
         if (st == VJ_OK) st = vj_detector_occupancy(d, &fit);
         if (st != VJ_OK) break;
-        dc.blocksPerSM = c.blocksPerSM > 0 ? c.blocksPerSM : std::max(1, fit / c.workers);
+        dc.blocksPerSM = c.blocksPerSM > 0 ? c.blocksPerSM : fit;
         st = vj_detector_set_config(d, &dc);
+        // full-residency kernels take turns on the device; split ones may overlap
+        if (st == VJ_OK && dc.blocksPerSM * c.workers > fit) st = detector_set_launch_chain(d, &S->chain);
         if (st == VJ_OK) st = vj_detector_reserve(d, S->workerBudget);
         if (st != VJ_OK) break;
         cudaStream_t s = nullptr;
@@ -379,6 +386,7 @@ int vj_server_destroy(vj_server* s) {
     for (auto& t : s->threads) t.join();
     for (auto* d : s->dets) vj_detector_destroy(d);
     for (auto st : s->streams) cudaStreamDestroy(st);
+    if (s->chain.last) cudaEventDestroy(s->chain.last);
     {
         std::lock_guard<std::mutex> lk(s->mu);
         for (auto& kv : s->live)
