@@ -336,3 +336,24 @@ def test_detect_rejects_bad_input(cuda, vj, basic_pool, gin):
     assert e.detectMultiScale(img, 32, 32, 32, scaleFactor=1.0)[0] == vj.Status.kInvalidArg
     s, d = e.detectMultiScale(np.zeros((20, 20), np.uint8), 20, 20, 20)
     assert s == 0 and len(d) == 0  # smaller than the window: no level
+
+
+def test_device_grouping_grows_its_scratch(cuda, vj, oracle, basic_pool):
+    """A cascade that accepts every window through the variance gate: raw
+    detections far outnumber the grouping slots the queue buffers first hold,
+    so the launch reports the overflow, the detector grows the queues and
+    repeats it, and the grouped result still equals the oracle's."""
+    st = np.zeros(1, dtype=vj.STUMP4)
+    st[0] = (np.int32(7).view(np.float32), np.float32(0.0), np.float32(1.0), np.float32(1.0))
+    sg = np.zeros(1, dtype=vj.STAGE)
+    sg[0] = (0, 1, np.float32(-1e30))
+    scene = vj.synth_scene(21, 320, 240, 2, 24, 80)
+    e = detector(vj, basic_pool, st, sg)
+    s, grp = e.detectMultiScale(scene, 320, 240, 320, 1.25, 3, 24, 200000)
+    k = e.lastStats()
+    assert s == 0 and k["attempts"] >= 2 and k["rawDetections"] > 50000
+    ref = oracle.detect(basic_pool, st, sg, scene, threads=8)
+    assert len(ref) == k["rawDetections"]
+    assert grp.tobytes() == oracle.group_first_order(ref, 3, 0.2).tobytes()
+    s, grp2 = e.detectMultiScale(scene, 320, 240, 320, 1.25, 3, 24, 200000)
+    assert s == 0 and e.lastStats()["attempts"] == 1 and grp2.tobytes() == grp.tobytes()
