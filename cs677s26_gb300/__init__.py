@@ -28,7 +28,7 @@ from ._capi import (DETECTION, FEATURE_BEST, HAAR_FEATURE, STAGE, STAGE_CALIB, S
                     VJError, call, load, ptr)
 
 __all__ = ["Status", "FeatureMode", "FaceVisionEngine", "AdaBoostTrainer", "ModelIO", "VJError", "DetectServer",
-           "estimate_detect_bytes",
+           "estimate_detect_bytes", "crop_resize_batch",
            "HAAR_FEATURE", "STUMP4", "STAGE", "DETECTION", "TILE_BEST", "WEAK", "FEATURE_BEST",
            "STAGE_CALIB", "synth_patches", "synth_scene", "synth_cascade", "feature_pool", "load"]
 
@@ -265,6 +265,26 @@ def estimate_detect_bytes(w: int, h: int, scaleFactor: float = 1.25, minObjectSi
     call("vj_detect_estimate_bytes", int(win[0]), int(win[1]), int(w), int(h), C.c_float(scaleFactor),
          minObjectSize, maxDetections, C.byref(b))
     return b.value
+
+
+def crop_resize_batch(images, boxes, image_of, out_size: int = 24, d_out=None, stream=None):
+    """cropResizeTo24 (main.cu:245-284) on the device: crop k is Detection
+    boxes[k] of images[image_of[k]] (2-D uint8 CUDA tensors), resized to
+    out_size x out_size.  Returns (status, patches) with patches a CUDA uint8
+    tensor of shape (len(boxes), out_size, out_size)."""
+    import torch
+    boxes = np.ascontiguousarray(boxes, dtype=DETECTION)
+    image_of = np.ascontiguousarray(image_of, dtype=np.int32)
+    n = len(images)
+    ptrs = (C.c_void_p * n)(*[int(im.data_ptr()) for im in images])
+    ws = (C.c_int * n)(*[int(im.shape[1]) for im in images])
+    hs = (C.c_int * n)(*[int(im.shape[0]) for im in images])
+    ss = (C.c_int * n)(*[int(im.stride(0)) for im in images])
+    if d_out is None:
+        d_out = torch.empty((len(boxes), out_size, out_size), dtype=torch.uint8, device=images[0].device)
+    st = _capi.status("vj_crop_resize_batch", n, ptrs, ws, hs, ss, len(boxes), ptr(image_of), ptr(boxes),
+                      out_size, int(d_out.data_ptr()) if len(boxes) else None, _stream(stream))
+    return Status(st), d_out
 
 
 class DetectServer:

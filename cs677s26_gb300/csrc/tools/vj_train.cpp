@@ -25,7 +25,9 @@
 // program's own sampler (a square of side uniform in [24, min(w, h)] at a
 // uniform position, resized with the reference's crop-resize) instead of the
 // reference's Python script; the PGM list is sorted before its seeded
-// shuffle, so the order does not depend on the file system.  Setting
+// shuffle, so the order does not depend on the file system.  The mined
+// windows are cropped on the device (vj_crop_resize_batch) from the batch's
+// images, which are uploaded once for detection and cropping.  Setting
 // VJ_TRAIN_DUMP=<dir> writes each stage's training patches (positives, then
 // negatives) to <dir>/stageNN.bin.
 #include <algorithm>
@@ -353,6 +355,11 @@ int main(int argc, char** argv) {
             std::shuffle(order.begin(), order.end(), mineRng);
             const int capPer = std::max(20000, numNeg * 2);
             std::vector<vj_detection> out(static_cast<size_t>(kMineBatch) * capPer);
+            // a batch's images go to the device once: detection reads them
+            // there and the chosen windows are cropped there
+            DevArray<uint8_t> dBatch, dPatches;
+            if (!dPatches.alloc(static_cast<size_t>(kMineBatch) * kPerImageKeep * kPix))
+                return fail("mining patch buffer");
             int scanned = 0;
             for (size_t pos = 0; pos < order.size() && hard < numNeg;) {
                 std::vector<Gray> batch;
@@ -367,26 +374,56 @@ int main(int argc, char** argv) {
                 const int bn = static_cast<int>(batch.size());
                 std::vector<const uint8_t*> ptrs(bn);
                 std::vector<int> ws(bn), hs(bn), counts(bn);
+                size_t bytes = 0;
+                for (int i = 0; i < bn; ++i) bytes += static_cast<size_t>(batch[i].w) * batch[i].h;
+                if (bytes > dBatch.n) {
+                    cudaFree(dBatch.p);
+                    dBatch.p = nullptr;
+                    if (!dBatch.alloc(bytes)) return fail("mining image buffer");
+                }
+                size_t off = 0;
                 for (int i = 0; i < bn; ++i) {
-                    ptrs[i] = batch[i].px.data();
+                    ptrs[i] = dBatch.p + off;
                     ws[i] = batch[i].w;
                     hs[i] = batch[i].h;
+                    if (!cuda_ok(cudaMemcpy(dBatch.p + off, batch[i].px.data(), batch[i].px.size(),
+                                            cudaMemcpyHostToDevice), "mining image"))
+                        return 1;
+                    off += batch[i].px.size();
                 }
-                if (vj_detect_batch(miner, bn, ptrs.data(), ws.data(), hs.data(), ws.data(), 0, scaleFactor, 0, kWin,
+                if (vj_detect_batch(miner, bn, ptrs.data(), ws.data(), hs.data(), ws.data(), 1, scaleFactor, 0, kWin,
                                     capPer, 0, out.data(), capPer, counts.data(), nullptr) != VJ_OK)
                     return fail("mining detectMultiScale");
-                for (int i = 0; i < bn && hard < numNeg; ++i) {
+                // the top windows by score of each image, in image order, up to numNeg in all
+                std::vector<vj_detection> boxes;
+                std::vector<int> imageOf;
+                std::vector<int> scannedAt;  // crops chosen when each image is scanned
+                int chosen = hard;
+                for (int i = 0; i < bn && chosen < numNeg; ++i) {
                     vj_detection* d = out.data() + static_cast<size_t>(i) * capPer;
                     const int keep = std::min(counts[i], kPerImageKeep);
                     std::partial_sort(d, d + keep, d + counts[i],
                                       [](const vj_detection& a, const vj_detection& b) { return a.score > b.score; });
-                    for (int k = 0; k < keep && hard < numNeg; ++k)
-                        crop_resize(batch[i], d[k].x, d[k].y, d[k].w, d[k].h, kWin,
-                                    negDst + static_cast<size_t>(hard++) * kPix);
-                    if ((++scanned % 20) == 0)
-                        std::cout << "[MINE] stage=" << stageIdx << " scanned=" << scanned << " hard=" << hard << "/"
-                                  << numNeg << "\n";
+                    for (int k = 0; k < keep && chosen < numNeg; ++k, ++chosen) {
+                        boxes.push_back(d[k]);
+                        imageOf.push_back(i);
+                    }
+                    scannedAt.push_back(chosen);
                 }
+                const int nc = static_cast<int>(boxes.size());
+                if (nc > 0) {
+                    if (vj_crop_resize_batch(bn, ptrs.data(), ws.data(), hs.data(), ws.data(), nc, imageOf.data(),
+                                             boxes.data(), kWin, dPatches.p, nullptr) != VJ_OK)
+                        return fail("mining cropResizeTo24");
+                    if (!cuda_ok(cudaMemcpy(negDst + static_cast<size_t>(hard) * kPix, dPatches.p,
+                                            static_cast<size_t>(nc) * kPix, cudaMemcpyDeviceToHost), "mined patches"))
+                        return 1;
+                }
+                for (const int c : scannedAt)
+                    if ((++scanned % 20) == 0)
+                        std::cout << "[MINE] stage=" << stageIdx << " scanned=" << scanned << " hard=" << c << "/"
+                                  << numNeg << "\n";
+                hard += nc;
             }
             std::cout << "[TRAIN] stage=" << stageIdx << " hardNegSelected=" << hard << "/" << numNeg << "\n";
         }

@@ -380,6 +380,18 @@ int vj_detect(vj_detector* d, const uint8_t* image, int w, int h, int stride,
 int vj_group_rectangles(const vj_detection* in, int n, int minNeighbors, float eps,
                         vj_detection* out, int* count);
 
+/* cropResizeTo24 (main.cu:245-284), the hard-negative miner's crop, on the
+ * device for many windows: crop k is the rectangle (x, y, w, h) of boxes[k]
+ * (a Detection; max(1, w) by max(1, h), clamped at the border) of image
+ * imageOf[k], resized with pixel-centre bilinear interpolation to
+ * outSize x outSize bytes at d_out + k * outSize * outSize (outSize 24 is the
+ * reference's).  images[i] are device pointers of w[i] x h[i] pixels with row
+ * stride stride[i]; the other arrays are host arrays.  Asynchronous on the
+ * stream. */
+int vj_crop_resize_batch(int nImages, const uint8_t* const* images, const int* w, const int* h,
+                         const int* stride, int nCrops, const int* imageOf, const vj_detection* boxes,
+                         int outSize, uint8_t* d_out, void* stream);
+
 /* Batched detection of n images in one pass (no reference counterpart; each
  * image's result equals vj_detect on that image alone).  All pyramid levels of
  * all images are scanned by one persistent kernel launch, replayed from a

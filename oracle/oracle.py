@@ -71,6 +71,8 @@ def lib() -> C.CDLL:
         L.vjo_group.argtypes = [vp, i32, i32, f32, vp]
         L.vjo_group_first_order.restype = i32
         L.vjo_group_first_order.argtypes = [vp, i32, i32, f32, vp]
+        L.vjo_crop_resize.restype = None
+        L.vjo_crop_resize.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp]
         _lib = L
     return _lib
 
@@ -90,6 +92,7 @@ def ref() -> C.CDLL:
         R.ref_integral.argtypes = [vp, i32, i32, i32, vp, vp, vp]
         R.ref_weak_search.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp, vp, vp]
         R.ref_resize.argtypes = [vp, i32, i32, i32, vp, i32, i32]
+        R.ref_crop.argtypes = [vp, i32, i32, i32, i32, i32, i32, vp]
         R.ref_detect.restype = i32
         R.ref_detect.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, i32, i32, f32, i32, i32, i32, vp, i32]
         R.ref_group.restype = i32
@@ -193,3 +196,12 @@ def group_first_order(dets, min_neighbors=4, eps=0.2):
     out = np.zeros(max(1, len(dets)), dtype=DET)
     n = lib().vjo_group_first_order(_p(dets), len(dets), min_neighbors, eps, _p(out))
     return out[:n].copy()
+
+
+def crop_resize(img, box, out=24):
+    """cropResizeTo24 of box = (x, y, w, h) from a 2-D uint8 image."""
+    img = np.ascontiguousarray(img, dtype=np.uint8)
+    dst = np.zeros((out, out), np.uint8)
+    x, y, w, h = (int(v) for v in box)
+    lib().vjo_crop_resize(_p(img), img.shape[1], img.shape[0], img.shape[1], x, y, w, h, out, _p(dst))
+    return dst

@@ -11,6 +11,7 @@
 //   detectMultiScaleCpu    main.cu:684-827
 //   groupRectanglesCpu     face_vision_engine.cu:1401-1539
 //   ModelIO save/load      model_io.cpp:66-167
+//   cropResizeTo24         main.cu:245-284
 #include <algorithm>
 #include <array>
 #include <chrono>
@@ -116,6 +117,22 @@ int ref_model_save(const char* path, const vj::HaarFeature* f, long long nf, con
     std::vector<vj::GpuStump4> vs(s, s + ns);
     std::vector<vj::CascadeStage> vst(st, st + nst);
     return vj::ModelIO::saveCascadeModel(path, vj::WindowSpec{24, 24}, vf, vs, vst) ? 1 : 0;
+}
+
+// cropResizeTo24 of the window (x, y, bw, bh) of a w x h image (no row padding).
+void ref_crop(const uint8_t* img, int w, int h, int x, int y, int bw, int bh, uint8_t* out24) {
+    GrayImage g;
+    g.w = w;
+    g.h = h;
+    g.data.assign(img, img + static_cast<size_t>(w) * h);
+    vj::Detection d{};
+    d.x = x;
+    d.y = y;
+    d.w = bw;
+    d.h = bh;
+    std::vector<uint8_t> o;
+    cropResizeTo24(g, d, o);
+    std::memcpy(out24, o.data(), o.size());
 }
 
 }  // extern "C"

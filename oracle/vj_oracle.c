@@ -918,3 +918,35 @@ int vjo_group_first_order(const vjo_det* in, int n, int minNeighbors, float eps,
     free(pos);
     return k;
 }
+
+/* ------------------------------------------------------------------------ */
+/* cropResizeTo24: main.cu:245-284.  Every operation is one IEEE single      */
+/* rounding in the reference's order (compiled with -ffp-contract=off).      */
+/* ------------------------------------------------------------------------ */
+
+void vjo_crop_resize(const uint8_t* img, int w, int h, int stride, int x, int y, int bw, int bh, int out,
+                     uint8_t* dst) {
+    const float sx = (float)(bw > 1 ? bw : 1);
+    const float sy = (float)(bh > 1 ? bh : 1);
+    const float stepX = sx / (float)out, stepY = sy / (float)out;
+    for (int oy = 0; oy < out; ++oy) {
+        for (int ox = 0; ox < out; ++ox) {
+            const float fx = (float)x + ((float)ox + 0.5f) * stepX - 0.5f;
+            const float fy = (float)y + ((float)oy + 0.5f) * stepY - 0.5f;
+            int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+            x0 = x0 < 0 ? 0 : (x0 > w - 1 ? w - 1 : x0);
+            y0 = y0 < 0 ? 0 : (y0 > h - 1 ? h - 1 : y0);
+            const int x1 = x0 + 1 < w - 1 ? x0 + 1 : w - 1;
+            const int y1 = y0 + 1 < h - 1 ? y0 + 1 : h - 1;
+            const float ax = fx - (float)x0, ay = fy - (float)y0;
+            const float p00 = (float)img[(size_t)y0 * stride + x0], p01 = (float)img[(size_t)y0 * stride + x1];
+            const float p10 = (float)img[(size_t)y1 * stride + x0], p11 = (float)img[(size_t)y1 * stride + x1];
+            const float top = p00 + (p01 - p00) * ax;
+            const float bot = p10 + (p11 - p10) * ax;
+            const float val = top + (bot - top) * ay;
+            int v = (int)(val + 0.5f);
+            v = v < 0 ? 0 : (v > 255 ? 255 : v);
+            dst[(size_t)oy * out + ox] = (uint8_t)v;
+        }
+    }
+}

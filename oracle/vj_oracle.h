@@ -109,6 +109,12 @@ int vjo_detect(const vjo_feature* feats, int nFeat, const vjo_stump* stumps, int
 
 /* groupRectanglesCpu, face_vision_engine.cu:1401-1539.  Returns the count. */
 int vjo_group(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out);
+/* cropResizeTo24 (main.cu:245-284) generalised to an out x out patch: the
+ * window (x, y, bw, bh) of a w x h image with row stride `stride`, pixel-centre
+ * bilinear, clamped at the image border. */
+void vjo_crop_resize(const uint8_t* img, int w, int h, int stride, int x, int y, int bw, int bh, int out,
+                     uint8_t* dst);
+
 /* vjo_group with the output ordered by each cluster's first member (smallest
  * input index). */
 int vjo_group_first_order(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out);

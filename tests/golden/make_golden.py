@@ -3,7 +3,7 @@
 The reference (hengyizhu/CS677s26) ships no tests or golden vectors, so these
 are outputs of its CPU paths - buildHaarFeaturePool, buildHostIntegralImage,
 runCpuWeakSearch, resizeGrayBilinearHost, detectMultiScaleCpu,
-groupRectanglesCpu and ModelIO::saveCascadeModel - compiled from its sources
+groupRectanglesCpu, cropResizeTo24 and ModelIO::saveCascadeModel - compiled from its sources
 by oracle/Makefile into oracle/_ref/libvjref.so (only where the sources are,
 i.e. not on the GPU machines).  Inputs are seeded numpy arrays (stored in
 inputs.npz) or the package's synthetic generators (their bytes are hashed in
@@ -184,6 +184,21 @@ def main() -> None:
                       scene.ctypes.data, 320, 240, 320, 1.25, 24, 50, 0, out.ctypes.data, 50)
     inputs["det_trunc"] = out[:nd].copy()
     gold["detect_trunc"] = {"maxDetections": 50, "raw": int(nd)}
+
+    # ---- cropResizeTo24 of hard-negative windows (main.cu:245-284)
+    img = V.synth_scene(300, 203, 151, 2, 24, 100)
+    boxes = [(0, 0, 24, 24), (10, 5, 48, 48), (150, 100, 50, 50), (202, 150, 1, 1), (5, 7, 0, 0),
+             (37, 11, 31, 17), (-3, -2, 30, 30), (0, 0, 203, 151), (120, 80, 90, 90), (3, 4, 25, 26),
+             (60, 40, 23, 23), (100, 30, 300, 7)]
+    boxes += [(int(rng.integers(-20, 210)), int(rng.integers(-20, 160)), int(rng.integers(0, 240)),
+               int(rng.integers(0, 180))) for _ in range(52)]
+    crops = np.zeros((len(boxes), 576), np.uint8)
+    for k, (x, y, bw, bh) in enumerate(boxes):
+        R.ref_crop(img.ctypes.data, 203, 151, x, y, bw, bh, crops[k].ctypes.data)
+    inputs["crop_img"] = img
+    inputs["crop_boxes"] = np.array(boxes, np.int32)
+    inputs["crop_out"] = crops
+    gold["crop"] = {"boxes": len(boxes), "out_sha256": sha(crops)}
 
     # ---- model file bytes
     with tempfile.TemporaryDirectory() as td:

@@ -357,3 +357,41 @@ def test_device_grouping_grows_its_scratch(cuda, vj, oracle, basic_pool):
     assert grp.tobytes() == oracle.group_first_order(ref, 3, 0.2).tobytes()
     s, grp2 = e.detectMultiScale(scene, 320, 240, 320, 1.25, 3, 24, 200000)
     assert s == 0 and e.lastStats()["attempts"] == 1 and grp2.tobytes() == grp.tobytes()
+
+
+def test_crop_resize_batch(cuda, vj, oracle, gin):
+    """Device cropResizeTo24 against the reference's outputs (golden), and
+    against the oracle for windows of several images in one launch, with
+    padded rows and other output sizes."""
+    torch = cuda
+    img, boxes, out = gin["crop_img"], gin["crop_boxes"], gin["crop_out"]
+    dets = np.zeros(len(boxes), dtype=vj.DETECTION)
+    for k, (x, y, w, h) in enumerate(boxes):
+        dets[k]["x"], dets[k]["y"], dets[k]["w"], dets[k]["h"] = x, y, w, h
+    d_img = torch.from_numpy(img).cuda()
+    s, patches = vj.crop_resize_batch([d_img], dets, np.zeros(len(boxes), np.int32))
+    torch.cuda.synchronize()
+    assert s == 0 and np.array_equal(patches.cpu().numpy().reshape(len(boxes), -1), out)
+    # several images, one of them a view with padded rows
+    scenes = [vj.synth_scene(40 + i, 80 + 37 * i, 60 + 23 * i, 1, 24, 50) for i in range(3)]
+    padded = torch.zeros((scenes[1].shape[0], scenes[1].shape[1] + 29), dtype=torch.uint8, device="cuda")
+    padded[:, : scenes[1].shape[1]] = torch.from_numpy(scenes[1]).cuda()
+    dev = [torch.from_numpy(scenes[0]).cuda(), padded[:, : scenes[1].shape[1]], torch.from_numpy(scenes[2]).cuda()]
+    rng = np.random.default_rng(3)
+    n = 300
+    image_of = rng.integers(0, 3, n).astype(np.int32)
+    dets = np.zeros(n, dtype=vj.DETECTION)
+    for k in range(n):
+        H, W = scenes[image_of[k]].shape
+        dets[k]["x"], dets[k]["y"] = rng.integers(-10, W), rng.integers(-10, H)
+        dets[k]["w"], dets[k]["h"] = rng.integers(0, 2 * W), rng.integers(0, 2 * H)
+    for size in (24, 19):
+        s, patches = vj.crop_resize_batch(dev, dets, image_of, out_size=size)
+        torch.cuda.synchronize()
+        got = patches.cpu().numpy()
+        assert s == 0
+        for k in range(n):
+            b = (dets[k]["x"], dets[k]["y"], dets[k]["w"], dets[k]["h"])
+            assert np.array_equal(got[k], oracle.crop_resize(scenes[image_of[k]], b, out=size)), (size, k)
+    s, _ = vj.crop_resize_batch(dev, dets[:1], np.array([5], np.int32))
+    assert s == vj.Status.kInvalidArg

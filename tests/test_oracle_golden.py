@@ -131,3 +131,12 @@ def test_stage_calibration_rules(oracle):
     cut_idx = 500 - int(np.ceil(np.float32(0.99) * np.float32(500)))
     assert c["cutVal"] == ps[cut_idx]
     assert c["posPass"] >= 495 or c["strictGt"] == 0
+
+
+def test_crop_resize(oracle, golden, gin):
+    """cropResizeTo24 (main.cu:245-284): the oracle against the reference's own
+    function on border, empty, non-square, oversized and random windows."""
+    img, boxes, out = gin["crop_img"], gin["crop_boxes"], gin["crop_out"]
+    assert len(boxes) == golden["crop"]["boxes"]
+    for k, b in enumerate(boxes):
+        assert np.array_equal(oracle.crop_resize(img, b).reshape(-1), out[k]), tuple(b)
