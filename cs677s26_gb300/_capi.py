@@ -83,6 +83,7 @@ SIGNATURES = {
     "vj_integral_image": (i32, [vp, i32, i32, i32, vp, vp, vp]),
     "vj_integral_image_noalloc": (i32, [vp, i32, i32, i32, vp, vp, vp]),
     "vj_crop_resize_batch": (i32, [i32, vp, vp, vp, vp, i32, vp, vp, i32, vp, vp]),
+    "vj_trainer_set_stage_gate": (i32, [vp, vp]),
     "vj_trainer_create": (i32, [i32, i32, i32, C.POINTER(vp)]),
     "vj_trainer_destroy": (i32, [vp]),
     "vj_trainer_set_features": (i32, [vp, vp, i64]),

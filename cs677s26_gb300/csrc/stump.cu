@@ -51,6 +51,15 @@ constexpr int kRefineThreads = 256;
 constexpr int kRefineWarps = kRefineThreads / 32;
 constexpr float kU = 5.9604645e-08f;    // 2^-24, unit roundoff of FP32
 
+// Stage gate (vj_trainer_set_stage_gate): a device word that the round
+// kernels read first; once nonzero, every later round kernel returns at once.
+// The round update closes it with 2 when the search found no valid stump, the
+// calibration with 1 when the stage meets its targets, so a host can queue a
+// stage's rounds without reading anything back between them.
+__device__ __forceinline__ bool gate_closed(const int* g) {
+    return g != nullptr && *reinterpret_cast<const volatile int*>(g) != 0;
+}
+
 struct RoundParams {
     float tp, tn, w;             // active positive / negative weight and their sum
     float window;                // candidate window above the fast minimum
@@ -232,7 +241,8 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
 __global__ void __launch_bounds__(1024)
 prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
                   const float* __restrict__ weight, int n, float* __restrict__ wsg,
-                  RoundParams* __restrict__ prm) {
+                  RoundParams* __restrict__ prm, const int* gate) {
+    if (gate_closed(gate)) return;
     __shared__ double sp[32], sn[32];
     __shared__ int cp[32], cn[32];
     double tp = 0.0, tn = 0.0;
@@ -304,7 +314,8 @@ __global__ void __launch_bounds__(kSweepThreads, 2)
 sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
              int64_t gapStride, const float* __restrict__ wsgG, int n, int featCount,
              const uint8_t* __restrict__ usedMask, RoundParams* __restrict__ prm,
-             float* __restrict__ fastErr) {
+             float* __restrict__ fastErr, const int* gate) {
+    if (gate_closed(gate)) return;
     extern __shared__ float wsgS[];
     const float* wsg = wsgG;
     if (kSmemW) {
@@ -445,7 +456,8 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t
 // 3. Candidate selection.
 // ---------------------------------------------------------------------------
 __global__ void select_candidates_kernel(const float* __restrict__ fastErr, int featCount,
-                                         RoundParams* __restrict__ prm, int* __restrict__ cand) {
+                                         RoundParams* __restrict__ prm, int* __restrict__ cand, const int* gate) {
+    if (gate_closed(gate)) return;
     const float lim = __fadd_rn(__uint_as_float(prm->fastMinBits), prm->window);
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < featCount; f += gridDim.x * blockDim.x) {
         const float e = fastErr[f];
@@ -463,7 +475,9 @@ template <bool kSmemW>
 __global__ void __launch_bounds__(kRefineThreads)
 refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
               int64_t gapStride, const float* __restrict__ wsgG, int n, RoundParams* __restrict__ prm,
-              const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit) {
+              const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit,
+              const int* gate) {
+    if (gate_closed(gate)) return;
     extern __shared__ float wsgS[];
     __shared__ __align__(16) float stage[kRefineWarps][256];   // gathered weights of one chunk, in order
     __shared__ __align__(16) float2 pre[kRefineWarps][256];    // (left positive, left negative) after each position
@@ -598,7 +612,8 @@ __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const
                                 const float* __restrict__ invNorm, int n, const uint16_t* __restrict__ ord,
                                 int64_t ordStride, RoundParams* __restrict__ prm,
                                 const int8_t* __restrict__ refParity, const int* __restrict__ refSplit,
-                                vj_tile_best* __restrict__ out) {
+                                vj_tile_best* __restrict__ out, const int* gate) {
+    if (gate_closed(gate)) return;
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     vj_tile_best b;
     b.pad0 = b.pad1 = b.pad2 = 0;
@@ -638,7 +653,8 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
                     const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
                     float* __restrict__ weight, float* __restrict__ strong, int n,
                     uint8_t* __restrict__ usedMask, vj_weak_classifier* __restrict__ weakOut,
-                    int* __restrict__ status) {
+                    int* __restrict__ status, int* gate) {
+    if (gate_closed(gate)) return;
     __shared__ double part[1024];
     __shared__ vj_haar_feature sfeat;
     __shared__ float sTheta, sLeft, sRight;
@@ -675,6 +691,7 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
             if (usedMask) usedMask[b.featureIdx] = 1;
         }
         if (status) *status = valid ? 0 : 1;
+        if (!valid && gate) *gate = 2;
     }
     __syncthreads();
     if (!sValid) return;
@@ -723,7 +740,8 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
 __global__ void __launch_bounds__(1024)
 stage_calib_kernel(const float* __restrict__ strong, const uint8_t* __restrict__ active, int n,
                    int numPos, float minHitRate, float maxFalseAlarm, int stageNegBase,
-                   vj_stage_calib* __restrict__ out) {
+                   vj_stage_calib* __restrict__ out, int* gate) {
+    if (gate_closed(gate)) return;
     __shared__ uint32_t hist[256];
     __shared__ uint32_t sPrefix, sK;
     __shared__ int cnt[4];
@@ -791,6 +809,7 @@ stage_calib_kernel(const float* __restrict__ strong, const uint8_t* __restrict__
         r.falseAlarm = __fdiv_rn(static_cast<float>(r.negSurvive), static_cast<float>(stageNegBase));
         r.satisfied = ((r.hitRate >= minHitRate && r.falseAlarm <= maxFalseAlarm) || r.negSurvive == 0) ? 1 : 0;
         *out = r;
+        if (r.satisfied && gate) *gate = 1;
     }
 }
 
@@ -1032,6 +1051,7 @@ struct vj_trainer {
     int* d_refSplit = nullptr;
     RoundParams* d_prm = nullptr;
     int* d_status = nullptr;
+    int* d_gate = nullptr;  // stage gate of the round kernels (caller's memory), or none
     int64_t scratchFeat = 0;
     int scratchN = 0;
 };
@@ -1203,6 +1223,12 @@ int vj_trainer_prepare_stage(vj_trainer* t, void* stream) {
     return ok();
 }
 
+int vj_trainer_set_stage_gate(vj_trainer* t, int* d_gate) {
+    if (!t) return set_error(VJ_INVALID_ARG, "vj_trainer_set_stage_gate: null trainer");
+    t->d_gate = d_gate;
+    return ok();
+}
+
 int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_out, void* stream) {
     int st = check_bound(t, "vj_stump_search");
     if (st != VJ_OK) return st;
@@ -1216,7 +1242,8 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
     if (st != VJ_OK) return st;
     const int F = static_cast<int>(t->nFeat), n = t->n;
     VJ_TIMED_LAUNCH("prep_round_kernel", s,
-                    prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, n, t->d_wsg, t->d_prm));
+                    prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, n, t->d_wsg, t->d_prm,
+                                                         t->d_gate));
     VJ_LAUNCH_CHECK("prep_round_kernel");
     const bool smemW = n <= kSmemWeightsMax;
     const size_t wbytes = smemW ? sizeof(float) * n : 0;
@@ -1226,24 +1253,26 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("sweep_kernel", s,
                         k<<<grid, kSweepThreads, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride,
-                                                             t->d_wsg, n, F, d_usedMask, t->d_prm, t->d_fastErr));
+                                                             t->d_wsg, n, F, d_usedMask, t->d_prm, t->d_fastErr,
+                                                             t->d_gate));
         VJ_LAUNCH_CHECK("sweep_kernel");
     }
     VJ_TIMED_LAUNCH("select_candidates_kernel", s,
                     select_candidates_kernel<<<std::min(div_up(F, 256), 4 * sm_count()), 256, 0, s>>>(
-                        t->d_fastErr, F, t->d_prm, t->d_cand));
+                        t->d_fastErr, F, t->d_prm, t->d_cand, t->d_gate));
     VJ_LAUNCH_CHECK("select_candidates_kernel");
     {
         auto k = smemW ? refine_kernel<true> : refine_kernel<false>;
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("refine_kernel", s,
                         k<<<2 * sm_count(), kRefineThreads, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg,
-                                                          n, t->d_prm, t->d_cand, t->d_refParity, t->d_refSplit));
+                                                          n, t->d_prm, t->d_cand, t->d_refParity, t->d_refSplit,
+                                                          t->d_gate));
         VJ_LAUNCH_CHECK("refine_kernel");
     }
     VJ_TIMED_LAUNCH("finalize_kernel", s,
                     finalize_kernel<<<1, 32, 0, s>>>(t->d_feat, t->d_sumT, t->d_invNorm, n, t->d_ord, t->ordStride,
-                                                     t->d_prm, t->d_refParity, t->d_refSplit, d_out));
+                                                     t->d_prm, t->d_refParity, t->d_refSplit, d_out, t->d_gate));
     VJ_LAUNCH_CHECK("finalize_kernel");
     return ok();
 }
@@ -1259,7 +1288,7 @@ int vj_round_update(vj_trainer* t, const vj_tile_best* d_best, float* d_strong, 
     VJ_TIMED_LAUNCH("round_update_kernel", s,
                     round_update_kernel<<<1, 1024, 0, s>>>(t->d_feat, d_best, t->d_sumT, t->d_invNorm, t->d_label,
                                                            t->d_active, t->d_weight, d_strong, t->n, d_usedMask,
-                                                           d_weak_out, t->d_status));
+                                                           d_weak_out, t->d_status, t->d_gate));
     VJ_LAUNCH_CHECK("round_update_kernel");
     return ok();
 }
@@ -1273,7 +1302,7 @@ int vj_stage_calibrate(vj_trainer* t, const float* d_strong, int numPos, float m
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VJ_TIMED_LAUNCH("stage_calib_kernel", s,
                     stage_calib_kernel<<<1, 1024, 0, s>>>(d_strong, t->d_active, t->n, numPos, minHitRate,
-                                                          maxFalseAlarm, stageNegBaseCount, d_out));
+                                                          maxFalseAlarm, stageNegBaseCount, d_out, t->d_gate));
     VJ_LAUNCH_CHECK("stage_calib_kernel");
     return ok();
 }
@@ -1313,7 +1342,7 @@ int vj_trainer_find_thresholds(vj_trainer* t, const float* d_resp, const uint16_
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VJ_TIMED_LAUNCH("prep_round_kernel", s,
                     prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, t->n, t->d_wsg,
-                                                         t->d_prm));
+                                                         t->d_prm, nullptr));
     VJ_LAUNCH_CHECK("prep_round_kernel");
     VJ_TIMED_LAUNCH("find_thresholds_kernel", s,
                     find_thresholds_kernel<<<div_up(featureCount, 8), 256, 0, s>>>(d_resp, d_sortedIdx, t->n,

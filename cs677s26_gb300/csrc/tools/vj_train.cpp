@@ -18,7 +18,9 @@
 //     maxWeakPerStage rounds and 6,061 weak classifiers in all;
 //   - the stage threshold stored is the calibrated one minus 1e-5f.
 // The rounds run on the device (stage-resident sorted orders, the exact
-// reference stump pick, FP64 renormalisation, on-device calibration); the
+// reference stump pick, FP64 renormalisation, on-device calibration) behind
+// the trainer's stage gate, so the host reads back once per 16 queued
+// rounds instead of after every round; the
 // mining runs as batched detection (vj_detect_batch over 32 images per launch).
 //
 // Differences, all in how negatives are sourced: random crops come from this
@@ -64,6 +66,7 @@ constexpr int kPix = kWin * kWin;
 constexpr int kMineBatch = 32;
 constexpr int kPerImageKeep = 256;
 constexpr int kMiningMax = 2048;
+constexpr int kRoundChunk = 16;  // boosting rounds queued per read of the stage gate
 
 bool load_raw_bin(const std::string& path, std::vector<uint8_t>& out, int& count) {
     std::ifstream ifs(path, std::ios::binary);
@@ -292,11 +295,14 @@ int main(int argc, char** argv) {
     DevArray<float> dInv, dWeight, dStrong;
     DevArray<int8_t> dLabel;
     DevArray<vj_tile_best> dBest;
-    DevArray<vj_weak_classifier> dWeak;
+    DevArray<vj_weak_classifier> dWeak;  // one record per round of a stage
     DevArray<vj_stage_calib> dCalib;
+    DevArray<int> dGate;
+    const int maxRounds = std::min(maxWeakPerStage, kTotalFeatures);
     if (!dTrain.alloc(static_cast<size_t>(n) * kPix) || !dActive.alloc(n) || !dUsed.alloc(static_cast<size_t>(nf)) ||
         !dSumT.alloc(static_cast<size_t>(625) * n) || !dInv.alloc(n) || !dWeight.alloc(n) || !dStrong.alloc(n) ||
-        !dLabel.alloc(n) || !dBest.alloc(1) || !dWeak.alloc(1) || !dCalib.alloc(1)) {
+        !dLabel.alloc(n) || !dBest.alloc(1) || !dWeak.alloc(static_cast<size_t>(maxRounds)) ||
+        !dCalib.alloc(static_cast<size_t>(maxRounds)) || !dGate.alloc(1)) {
         std::cerr << "[ERR] device allocation failed\n";
         return 1;
     }
@@ -469,22 +475,44 @@ int main(int argc, char** argv) {
         const int limit = std::min(maxWeakPerStage, kTotalFeatures - stageFirst);
         bool satisfied = false;
         float stageThreshold = 0.0f;
-        for (int r = 0; r < limit; ++r) {
-            if (vj_stump_search(tr, dUsed.p, dBest.p, nullptr) != VJ_OK) return fail("best-weak search");
-            vj_tile_best best{};
-            if (!cuda_ok(cudaMemcpy(&best, dBest.p, sizeof(best), cudaMemcpyDeviceToHost), "round best")) return 1;
-            if (!(best.featureIdx >= 0) || !std::isfinite(best.bestErr)) {
+        // The rounds run behind the trainer's stage gate, queued kRoundChunk
+        // at a time with one read of the gate per chunk: a round that finds
+        // no valid stump or meets the stage targets closes the gate and the
+        // rest of the queued rounds do nothing.  Unrun rounds keep featureIdx
+        // -1 in their weak record.
+        if (!cuda_ok(cudaMemset(dGate.p, 0, sizeof(int)), "gate") ||
+            !cuda_ok(cudaMemset(dWeak.p, 0xFF, sizeof(vj_weak_classifier) * static_cast<size_t>(limit)), "weak records"))
+            return 1;
+        if (vj_trainer_set_stage_gate(tr, dGate.p) != VJ_OK) return fail("stage gate");
+        int queued = 0, gate = 0;
+        while (queued < limit && gate == 0) {
+            const int end = std::min(limit, queued + kRoundChunk);
+            for (int r = queued; r < end; ++r) {
+                if (vj_stump_search(tr, dUsed.p, dBest.p, nullptr) != VJ_OK) return fail("best-weak search");
+                if (vj_round_update(tr, dBest.p, dStrong.p, dUsed.p, dWeak.p + r, nullptr) != VJ_OK)
+                    return fail("round update");
+                if (vj_stage_calibrate(tr, dStrong.p, numPos, minHitRate, maxFalseAlarm, numNeg, dCalib.p + r,
+                                       nullptr) != VJ_OK)
+                    return fail("stage calibration");
+            }
+            queued = end;
+            if (!cuda_ok(cudaMemcpy(&gate, dGate.p, sizeof(int), cudaMemcpyDeviceToHost), "gate")) return 1;
+        }
+        vj_trainer_set_stage_gate(tr, nullptr);
+        std::vector<vj_weak_classifier> roundWeak(static_cast<size_t>(queued));
+        std::vector<vj_stage_calib> roundCal(static_cast<size_t>(queued));
+        if (!cuda_ok(cudaMemcpy(roundWeak.data(), dWeak.p, sizeof(vj_weak_classifier) * roundWeak.size(),
+                                cudaMemcpyDeviceToHost), "weak records") ||
+            !cuda_ok(cudaMemcpy(roundCal.data(), dCalib.p, sizeof(vj_stage_calib) * roundCal.size(),
+                                cudaMemcpyDeviceToHost), "calibrations"))
+            return 1;
+        for (int r = 0; r < queued; ++r) {
+            const vj_weak_classifier& wk = roundWeak[static_cast<size_t>(r)];
+            const vj_stage_calib& cal = roundCal[static_cast<size_t>(r)];
+            if (wk.featureIdx < 0) {
                 std::cerr << "[WARN] No valid weak found at stage " << stageIdx << " weakRound " << r << "\n";
                 break;
             }
-            if (vj_round_update(tr, dBest.p, dStrong.p, dUsed.p, dWeak.p, nullptr) != VJ_OK) return fail("round update");
-            if (vj_stage_calibrate(tr, dStrong.p, numPos, minHitRate, maxFalseAlarm, numNeg, dCalib.p, nullptr) != VJ_OK)
-                return fail("stage calibration");
-            vj_weak_classifier wk{};
-            vj_stage_calib cal{};
-            if (!cuda_ok(cudaMemcpy(&wk, dWeak.p, sizeof(wk), cudaMemcpyDeviceToHost), "weak") ||
-                !cuda_ok(cudaMemcpy(&cal, dCalib.p, sizeof(cal), cudaMemcpyDeviceToHost), "calibration"))
-                return 1;
             weaks.push_back(wk);
             stageThreshold = cal.stageThreshold;
             std::cout << "[TRAIN] stage=" << stageIdx << " weak=" << r << " feature=" << wk.featureIdx

@@ -266,6 +266,18 @@ int vj_trainer_select_best_in_tile(vj_trainer* t, const vj_feature_best_split* d
                                    const uint8_t* d_usedMask, vj_tile_best* d_out,
                                    void* stream);
 
+/* Stage gate (no reference counterpart): d_gate is a device int (or NULL to
+ * turn gating off).  While it is nonzero, vj_stump_search, vj_round_update and
+ * vj_stage_calibrate launch kernels that return at once.  vj_round_update sets
+ * it to 2 when the search found no valid stump (nothing is updated, no weak
+ * classifier is written); vj_stage_calibrate sets it to 1 when the stage meets
+ * its targets (hit >= minHitRate and false alarm <= maxFalseAlarm, or no
+ * negative survives).  A caller zeroes it, queues a stage's rounds (or chunks
+ * of them) without reading anything back between them, and reads the gate and
+ * the per-round records afterwards - the reference's stage loop
+ * (main.cu:2005-2166) without a host round trip per round. */
+int vj_trainer_set_stage_gate(vj_trainer* t, int* d_gate);
+
 /* One boosting round's full best-weak search over the whole pool: the tile
  * loop of src/main.cu:2013-2053 plus ReduceTileBestCandidatesKernel
  * (main.cu:999-1028), fused.  The returned stump (feature, threshold, parity,

@@ -395,3 +395,53 @@ def test_crop_resize_batch(cuda, vj, oracle, gin):
             assert np.array_equal(got[k], oracle.crop_resize(scenes[image_of[k]], b, out=size)), (size, k)
     s, _ = vj.crop_resize_batch(dev, dets[:1], np.array([5], np.int32))
     assert s == vj.Status.kInvalidArg
+
+
+def test_stage_gate_queues_a_stage_without_reads(cuda, vj, oracle, basic_pool):
+    """Rounds queued behind the trainer's stage gate (vj_trainer_set_stage_gate)
+    equal rounds run one by one with a read after each, up to the round that
+    meets the stage targets; the gate then reads 1 and every queued round
+    after it leaves weights, scores, used mask and records untouched."""
+    torch = cuda
+    npos = nneg = 400
+    p = vj.synth_patches(17, npos, nneg)
+    labels = np.array([1] * npos + [-1] * nneg, np.int8)
+    w0 = np.where(labels > 0, np.float32(0.5) / np.float32(npos), np.float32(0.5) / np.float32(nneg))
+    w0 = (w0.astype(np.float64) / w0.astype(np.float64).sum()).astype(np.float32)
+    feats = np.ascontiguousarray(basic_pool[:30000])
+    rounds = 12
+    hit, fa = 0.995, 0.5
+
+    def run(gated):
+        T = Train(cuda, vj, oracle, p, labels, feats, w0)
+        assert T.t.prepareStage() == 0
+        weak = torch.full((rounds, 7), -1, dtype=torch.int32, device="cuda")
+        calib = torch.zeros((rounds, 8), dtype=torch.int32, device="cuda")
+        gate = torch.zeros(1, dtype=torch.int32, device="cuda")
+        h = T.t._h
+        if gated:
+            assert vj._capi.status("vj_trainer_set_stage_gate", h, gate.data_ptr()) == 0
+        snaps = []
+        for r in range(rounds):
+            assert vj._capi.status("vj_stump_search", h, T.used.data_ptr(), T.best.data_ptr(), None) == 0
+            assert vj._capi.status("vj_round_update", h, T.best.data_ptr(), T.strong.data_ptr(), T.used.data_ptr(),
+                                 weak[r].data_ptr(), None) == 0
+            assert vj._capi.status("vj_stage_calibrate", h, T.strong.data_ptr(), npos, C.c_float(hit), C.c_float(fa),
+                                 nneg, calib[r].data_ptr(), None) == 0
+            if not gated:
+                snaps.append((T.w.cpu().numpy().copy(), T.strong.cpu().numpy().copy(), T.used.cpu().numpy().copy()))
+        torch.cuda.synchronize()
+        if gated:
+            snaps.append((T.w.cpu().numpy().copy(), T.strong.cpu().numpy().copy(), T.used.cpu().numpy().copy()))
+        return weak.cpu().numpy(), calib.cpu().numpy(), snaps, int(gate.cpu().item())
+
+    wa, ca, sa, _ = run(False)
+    sat = [r for r in range(rounds) if ca[r].view(vj.STAGE_CALIB)[0]["satisfied"]]
+    assert sat and sat[0] < rounds - 1  # the targets are met before the last queued round
+    k = sat[0]
+    wb, cb, sb, g = run(True)
+    assert g == 1
+    assert np.array_equal(wb[: k + 1], wa[: k + 1]) and np.array_equal(cb[: k + 1], ca[: k + 1])
+    assert (wb[k + 1:] == -1).all() and (cb[k + 1:] == 0).all()
+    for x, y in zip(sb[0], sa[k]):
+        assert np.array_equal(x, y)
