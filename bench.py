@@ -309,13 +309,14 @@ def run_gpu(args, rank, world):
             "serving": "Poisson arrivals at 200, 1000 and 2000 req/s of requests drawn from the same 256 scenes, "
                        "the same trace for both servers; 16 GiB HBM budget each; plain = one image per launch "
                        "(maxBatchImages 1, one worker); batched = continuous batching, 2 workers whose kernels "
-                       "each fill the GPU and take turns, up to 256 images per launch"}
+                       "each fill the GPU and take turns, up to 256 images and 32 MP per launch"}
         result["detect"] = det
     return result
 
 
 # ----------------------------------------------------------------------------- detection and serving
 BATCH_SCENES = 256
+BATCH_PIXELS = 32_000_000  # serving batch cap: a few GPU-milliseconds of work, enough to fill the GPU
 
 
 def detect_inputs(V):
@@ -423,11 +424,11 @@ def run_detect(V, torch, quick=False):
     # ---- serving: Poisson arrivals of the same scenes at each rate, continuous
     # batching (2 workers, every kernel on the whole GPU, taking turns) against
     # plain per-image detect (one image per launch), same trace, same results
-    serving = {"hbm_budget_gb": (16 << 30) / 1e9, "workers": 2}
+    serving = {"hbm_budget_gb": (16 << 30) / 1e9, "workers": 2, "max_batch_pixels": BATCH_PIXELS}
     rates = [200] if quick else [200, 1000, 2000]
     plain = V.DetectServer(f, s, g, workers=1, maxBatchImages=1, hbmBudgetBytes=16 << 30)
-    batched = V.DetectServer(f, s, g, workers=2, maxBatchImages=256, hbmBudgetBytes=16 << 30,
-                             tileRows=cfg["tileRows"], tileStumps=cfg["tileStumps"])
+    batched = V.DetectServer(f, s, g, workers=2, maxBatchImages=256, maxBatchPixels=BATCH_PIXELS,
+                             hbmBudgetBytes=16 << 30, tileRows=cfg["tileRows"], tileStumps=cfg["tileStumps"])
     serve_trace(plain, scenes, 200, 32, 99)
     serve_trace(batched, scenes, 200, 64, 99)
 

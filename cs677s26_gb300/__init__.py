@@ -295,13 +295,13 @@ class DetectServer:
                  hbmBudgetBytes: int = 16 << 30, maxImage=(3840, 2160), scaleFactor: float = 1.25,
                  minNeighbors: int = 4, minObjectSize: int = 24, maxDetections: int = 200000,
                  applyGrouping: bool = True, blocksPerSM: int = 0, tileRows: int = 0, tileStumps: int = 0,
-                 win=(24, 24)):
+                 maxBatchPixels: int = 0, win=(24, 24)):
         cfg = np.zeros(1, dtype=_capi.SERVER_CONFIG)
         for k, v in dict(winW=win[0], winH=win[1], maxImageW=maxImage[0], maxImageH=maxImage[1], workers=workers,
                          maxBatchImages=maxBatchImages, hbmBudgetBytes=hbmBudgetBytes, scaleFactor=scaleFactor,
                          minNeighbors=minNeighbors, minObjectSize=minObjectSize, maxDetections=maxDetections,
                          applyGrouping=int(applyGrouping), blocksPerSM=blocksPerSM, tileRows=tileRows,
-                         tileStumps=tileStumps).items():
+                         tileStumps=tileStumps, maxBatchPixels=maxBatchPixels).items():
             cfg[k] = v
         self._keep = [np.ascontiguousarray(a) for a in (features, stumps, stages)]
         f, s, g = self._keep

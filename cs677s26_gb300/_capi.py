@@ -46,7 +46,8 @@ SERVER_CONFIG = np.dtype([("winW", "<i4"), ("winH", "<i4"), ("maxImageW", "<i4")
                           ("workers", "<i4"), ("maxBatchImages", "<i4"), ("hbmBudgetBytes", "<i8"),
                           ("scaleFactor", "<f4"), ("minNeighbors", "<i4"), ("minObjectSize", "<i4"),
                           ("maxDetections", "<i4"), ("applyGrouping", "<i4"), ("blocksPerSM", "<i4"),
-                          ("tileRows", "<i4"), ("tileStumps", "<i4")])
+                          ("tileRows", "<i4"), ("tileStumps", "<i4"),
+                          ("maxBatchPixels", "<i8")])
 SERVER_STATS = np.dtype([("submitted", "<i8"), ("completed", "<i8"), ("failed", "<i8"), ("batches", "<i8"),
                          ("meanBatchImages", "<f8"), ("meanMs", "<f8"), ("p50Ms", "<f8"), ("p99Ms", "<f8"),
                          ("p999Ms", "<f8"), ("maxMs", "<f8"), ("elapsedS", "<f8"), ("imagesPerS", "<f8"),
@@ -55,7 +56,7 @@ PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "gro
 HOST_PHASES = ("plan_upload", "wait", "post")
 
 assert DETECT_STATS.itemsize == 160 and DETECT_CONFIG.itemsize == 24
-assert SERVER_CONFIG.itemsize == 64 and SERVER_STATS.itemsize == 112
+assert SERVER_CONFIG.itemsize == 72 and SERVER_STATS.itemsize == 112
 assert HAAR_FEATURE.itemsize == 64 and STUMP4.itemsize == 16 and STAGE.itemsize == 12
 assert DETECTION.itemsize == 24 and TILE_BEST.itemsize == 16 and WEAK.itemsize == 28
 

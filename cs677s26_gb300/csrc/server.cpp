@@ -3,7 +3,8 @@
 // Threads: the callers of vj_server_submit / vj_server_wait, and one thread
 // per worker.  A worker owns a vj_detector and a CUDA stream.  When it is
 // free it takes, in arrival order, every queued request that fits its share
-// of the HBM budget and runs them as one vj_detect_batch launch (one
+// of the HBM budget (and the batch pixel cap, if set) and runs them as one
+// vj_detect_batch launch (one
 // persistent kernel over all their pyramid levels, grouping included);
 // requests that arrive while batches are on the GPU wait for the next free
 // worker.  By default every worker's kernel fills the GPU (all resident CTAs
@@ -85,6 +86,7 @@ struct Request {
     uint8_t* pix = nullptr;  // pinned copy, w x h, stride w
     int w = 0, h = 0;
     int64_t bytes = 0;       // admission estimate
+    int64_t pixels = 0;
     Clock::time_point tSubmit, tDone;
     bool done = false;
     int status = VJ_OK;
@@ -137,11 +139,14 @@ void worker_loop(vj_server* S, int wi) {
             std::unique_lock<std::mutex> lk(S->mu);
             S->cvWork.wait(lk, [&] { return S->stopping || !S->queue.empty(); });
             if (S->queue.empty()) return;  // stopping and drained
-            int64_t bytes = 0;
+            int64_t bytes = 0, pixels = 0;
             while (!S->queue.empty() && static_cast<int>(batch.size()) < c.maxBatchImages) {
                 const auto& r = S->queue.front();
-                if (!batch.empty() && bytes + r->bytes > S->workerBudget) break;
+                if (!batch.empty() && (bytes + r->bytes > S->workerBudget ||
+                                       (c.maxBatchPixels > 0 && pixels + r->pixels > c.maxBatchPixels)))
+                    break;
                 bytes += r->bytes;
+                pixels += r->pixels;
                 batch.push_back(r);
                 S->queue.pop_front();
             }
@@ -214,7 +219,7 @@ int vj_server_create(const vj_server_config* cfg, const vj_haar_feature* feature
     *out = nullptr;
     vj_server_config c = *cfg;
     if (c.workers < 1 || c.workers > 16 || c.maxBatchImages < 1 || c.hbmBudgetBytes <= 0 || !(c.scaleFactor > 1.0f) ||
-        c.minObjectSize < 1 || c.maxDetections < 1 || c.blocksPerSM < 0)
+        c.minObjectSize < 1 || c.maxDetections < 1 || c.blocksPerSM < 0 || c.maxBatchPixels < 0)
         return set_error(VJ_INVALID_ARG, "vj_server_create: bad configuration");
     auto S = std::make_unique<vj_server>();
     S->cfg = c;
@@ -278,6 +283,7 @@ int vj_server_submit(vj_server* s, const uint8_t* image, int w, int h, int strid
     r->w = w;
     r->h = h;
     r->bytes = bytes;
+    r->pixels = static_cast<int64_t>(w) * h;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->stopping) {

@@ -526,9 +526,12 @@ typedef struct vj_server_config {
     int32_t minObjectSize;
     int32_t maxDetections;
     int32_t applyGrouping;
-    int32_t blocksPerSM;           /* persistent CTAs per SM per worker; 0 = split evenly */
+    int32_t blocksPerSM;           /* persistent CTAs per SM per worker; 0 = all that fit,
+                                      with the workers' kernels taking turns on the device */
     int32_t tileRows;              /* launch shape (vj_detect_config); 0 = default */
     int32_t tileStumps;
+    int64_t maxBatchPixels;        /* pixels per batch at most (a lone larger image still
+                                      runs); 0 = no limit */
 } vj_server_config;
 
 typedef struct vj_server_stats {
