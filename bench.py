@@ -316,7 +316,7 @@ def run_gpu(args, rank, world):
 
 # ----------------------------------------------------------------------------- detection and serving
 BATCH_SCENES = 256
-BATCH_PIXELS = 32_000_000  # serving batch cap: a few GPU-milliseconds of work, enough to fill the GPU
+BATCH_PIXELS = 32_000_000  # serving batch cap: about 30 ms of device work, well past what fills the GPU
 
 
 def detect_inputs(V):
