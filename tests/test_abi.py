@@ -182,7 +182,7 @@ def test_server_config_is_validated(vj, basic_pool):
     st, sg = vj.synth_cascade(2)
     f, s, g = basic_pool.view(vj.HAAR_FEATURE), st.view(vj.STUMP4), sg.view(vj.STAGE)
     for bad in (dict(workers=0), dict(maxBatchImages=0), dict(hbmBudgetBytes=0), dict(scaleFactor=1.0),
-                dict(blocksPerSM=-1)):
+                dict(blocksPerSM=-1), dict(maxBatchPixels=-1)):
         with pytest.raises(vj.VJError) as ei:
             vj.DetectServer(f, s, g, **bad)
         assert ei.value.status == vj.Status.kInvalidArg

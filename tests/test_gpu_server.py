@@ -125,3 +125,24 @@ def test_poll_wait_and_unknown_ticket(cuda, vj, model, scenes):
         assert st == vj.Status.kInvalidArg
     finally:
         srv.close()
+
+
+def test_batch_pixel_cap(cuda, vj, model, scenes, alone):
+    """maxBatchPixels: a batch takes requests while their pixels fit the cap (a
+    lone larger image still runs), so a cap below every image gives one image
+    per batch and a cap of two small images at most two; results unchanged."""
+    f, s, g = model
+    small = sorted(range(len(scenes)), key=lambda i: scenes[i].size)[:8]
+    for cap, most in ((1, 1), (2 * max(scenes[i].size for i in small), 2)):
+        srv = vj.DetectServer(f, s, g, workers=1, maxBatchImages=64, maxBatchPixels=cap, hbmBudgetBytes=8 << 30)
+        try:
+            tickets = [srv.submit(scenes[i]) for i in small]
+            for i, t in zip(small, tickets):
+                st, d = srv.wait(t)
+                assert st == 0 and d.tobytes() == alone[i].tobytes()
+            k = srv.stats()
+            assert k["completed"] == len(small) and k["batches"] >= len(small) / most
+            if most == 1:
+                assert k["batches"] == len(small)
+        finally:
+            srv.close()
