@@ -252,7 +252,7 @@ const void* kernel_for(int blocksPerSM) {
 
 template <int TH>
 const void* kernel_for_slots(int blocksPerSM, int slots) {
-    return slots == 4 ? kernel_for<TH, 4>(blocksPerSM) : kernel_for<TH, 2>(blocksPerSM);
+    return slots == 1 ? kernel_for<TH, 1>(blocksPerSM) : kernel_for<TH, 2>(blocksPerSM);
 }
 
 // Kernel variant for a launch shape: tile rows, deep-pass window slots, and
@@ -807,9 +807,9 @@ int run_batch(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice,
 
 int check_config(const vj_detect_config& c) {
     if ((c.tileRows != 4 && c.tileRows != 8 && c.tileRows != 16) || c.tileStumps < 0 || c.queueStumps < 0 ||
-        c.blocksPerSM < 0 || (c.deepSlots != 2 && c.deepSlots != 4) || c.reserved != 0)
+        c.blocksPerSM < 0 || (c.deepSlots != 1 && c.deepSlots != 2) || c.reserved != 0)
         return set_error(VJ_INVALID_ARG,
-                         "detection config: tileRows must be 4, 8 or 16, deepSlots 2 or 4, the rest >= 0");
+                         "detection config: tileRows must be 4, 8 or 16, deepSlots 1 or 2, the rest >= 0");
     return VJ_OK;
 }
 
@@ -1154,7 +1154,7 @@ int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images, co
     };
     for (int th : {8, 4, 16})
         for (int bps : {4, 0})
-            for (int slots : {2, 4}) {
+            for (int slots : {2, 1}) {
                 if (st != VJ_OK) break;
                 vj_detect_config c = saved;
                 c.tileRows = th;

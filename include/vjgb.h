@@ -461,7 +461,8 @@ typedef struct vj_detect_config {
     int32_t blocksPerSM;  /* persistent CTAs per SM (0 = as many as fit); 4 or
                              more selects the kernel compiled for 4 CTAs per
                              SM (64 registers per thread) */
-    int32_t deepSlots;    /* windows a warp holds in the deep pass: 2 or 4 */
+    int32_t deepSlots;    /* windows a warp holds in the deep pass: 1 or 2 (1 halves
+                             the deep pass's shared memory, leaving more L1) */
     int32_t reserved;     /* 0 */
 } vj_detect_config;
 
