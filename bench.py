@@ -155,6 +155,57 @@ class Stage:
             assert self.t.calibrateStage(self.strong, self.numPos, 0.99, 0.4, NNEG, self.calib, stream) == 0
 
 
+def stump_responses(feat, sumT, inv):
+    """FP32 responses of one upright feature for every sample (exact int box
+    sums, one FP32 rounding by invNorm): the statement's own arithmetic."""
+    raw = np.zeros(sumT.shape[1], np.int64)
+    for r in ("r0", "r1", "r2")[: int(feat["rectCount"])]:
+        q = feat[r]
+        box = sumT[int(q["p0"])] - sumT[int(q["p1"])] - sumT[int(q["p2"])] + sumT[int(q["p3"])]
+        raw += box * np.int64(q["w"])
+    return (raw.astype(np.float32) * inv).astype(np.float32)
+
+
+def round_report(V, st, pool):
+    """One extra stage step, untimed, read back round by round: the pick's FP32
+    error (the reference's sequential FP32 search arithmetic) beside the FP64
+    weighted error of the same stump over that round's weights, and the FP32
+    gap from the pick to the runner-up among the exactly replayed candidates
+    (null when the pick was the only candidate)."""
+    V._capi.call("vj_integral_batch", st.d_p.data_ptr(), 24, 24, 24, st.n, st.sumT.data_ptr(), None,
+                 st.inv.data_ptr(), None)
+    st.w.copy_(st.w0)
+    st.strong.zero_()
+    st.used.zero_()
+    assert st.t.bindTrainingSet(st.ii, st.lab, None, st.w) == 0
+    assert st.t.prepareStage() == 0
+    sumT = st.sumT.cpu().numpy().reshape(625, st.n).astype(np.int64)
+    inv = st.inv.cpu().numpy()
+    rows = []
+    for r in range(ROUNDS):
+        w = st.w.cpu().numpy().astype(np.float64)
+        assert st.t.bestWeak(st.used, st.best) == 0
+        info = st.t.lastRound()
+        b = st.best.cpu().numpy().view(V.TILE_BEST)[0]
+        f, theta, par = int(b["featureIdx"]), np.float32(b["bestTheta"]), int(b["bestParity"])
+        left = stump_responses(pool[f], sumT, inv) < theta
+        pred = np.where(left, -1, 1) if par > 0 else np.where(left, 1, -1)
+        e64 = float(w[pred != st.h_labels].sum())
+        e32 = float(b["bestErr"])
+        ru = info["runnerUpErr"]
+        rows.append({"round": r, "featureIdx": f, "err_fp32": e32, "err_fp64": e64, "abs_diff": abs(e32 - e64),
+                     "runner_up_gap_fp32": (ru - e32) if np.isfinite(ru) else None,
+                     "candidates": info["candidates"], "window": info["window"]})
+        wk = st.weaks[r * 7:(r + 1) * 7]
+        assert st.t.applyBestWeak(st.best, st.strong, st.used, wk) == 0
+        assert st.t.calibrateStage(st.strong, st.numPos, 0.99, 0.4, NNEG, st.calib) == 0
+    gaps = [x["runner_up_gap_fp32"] for x in rows if x["runner_up_gap_fp32"] is not None]
+    return {"rounds": rows, "max_abs_err_diff": max(x["abs_diff"] for x in rows),
+            "min_runner_up_gap": min(gaps) if gaps else None,
+            "rounds_gap_below_diff": sum(1 for x in rows if x["runner_up_gap_fp32"] is not None and
+                                         x["runner_up_gap_fp32"] <= x["abs_diff"])}
+
+
 def profile_read(V, reset=True):
     import ctypes as C
     lib = V.load()
@@ -293,6 +344,8 @@ def run_gpu(args, rank, world):
     }
     if F != 162336 or ROUNDS != 50:
         result["config"]["workload"] = f"reduced stage step for profiling: {F} features, {ROUNDS} rounds"
+    if rank == 0:
+        result["round_report"] = round_report(V, st, pool)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(pool, patches)
     if dist:

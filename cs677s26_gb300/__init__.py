@@ -397,6 +397,13 @@ class AdaBoostTrainer:
         return Status(_capi.status("vj_stump_search", self._h, ptr(dUsedFeatureMask), ptr(dOut),
                                    _stream(stream)))
 
+    def lastRound(self) -> dict:
+        """Statistics of the last bestWeak: fast minimum, window, candidates, the
+        pick's and the runner-up's exact errors (vj_trainer_last_round)."""
+        rec = np.zeros(1, dtype=_capi.ROUND_INFO)
+        call("vj_trainer_last_round", self._h, ptr(rec))
+        return {k: rec[k][0].item() for k in _capi.ROUND_INFO.names}
+
     def applyBestWeak(self, dBest, dStrong, dUsedFeatureMask=None, dWeakOut=None, stream=None) -> int:
         return Status(_capi.status("vj_round_update", self._h, ptr(dBest), ptr(dStrong), ptr(dUsedFeatureMask),
                                    ptr(dWeakOut), _stream(stream)))

@@ -52,11 +52,14 @@ SERVER_STATS = np.dtype([("submitted", "<i8"), ("completed", "<i8"), ("failed", 
                          ("meanBatchImages", "<f8"), ("meanMs", "<f8"), ("p50Ms", "<f8"), ("p99Ms", "<f8"),
                          ("p999Ms", "<f8"), ("maxMs", "<f8"), ("elapsedS", "<f8"), ("imagesPerS", "<f8"),
                          ("peakAdmittedBytes", "<i8"), ("deviceBytes", "<i8")])
+ROUND_INFO = np.dtype([("fastMin", "<f4"), ("window", "<f4"), ("candidates", "<i4"), ("status", "<i4"),
+                       ("totalPos", "<f4"), ("totalNeg", "<f4"), ("bestErr", "<f4"), ("bestFeature", "<i4"),
+                       ("runnerUpErr", "<f4"), ("runnerUpFeature", "<i4")])
 PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "grouping", "output")
 HOST_PHASES = ("plan_upload", "wait", "post")
 
 assert DETECT_STATS.itemsize == 160 and DETECT_CONFIG.itemsize == 24
-assert SERVER_CONFIG.itemsize == 72 and SERVER_STATS.itemsize == 112
+assert SERVER_CONFIG.itemsize == 72 and SERVER_STATS.itemsize == 112 and ROUND_INFO.itemsize == 40
 assert HAAR_FEATURE.itemsize == 64 and STUMP4.itemsize == 16 and STAGE.itemsize == 12
 assert DETECTION.itemsize == 24 and TILE_BEST.itemsize == 16 and WEAK.itemsize == 28
 

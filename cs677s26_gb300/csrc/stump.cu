@@ -30,6 +30,7 @@
 // With vj_trainer_prepare_stage the orders of step 1 stay resident in HBM for
 // all rounds of a stage (the responses do not change within a stage, only
 // the weights), so a round costs steps 2-4 only.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -476,7 +477,7 @@ __global__ void __launch_bounds__(kRefineThreads)
 refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
               int64_t gapStride, const float* __restrict__ wsgG, int n, RoundParams* __restrict__ prm,
               const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit,
-              const int* gate) {
+              unsigned long long* __restrict__ candKey, const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ float wsgS[];
     __shared__ __align__(16) float stage[kRefineWarps][256];   // gathered weights of one chunk, in order
@@ -599,10 +600,14 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-        if (lane == 0 && best != ~0ull) {
-            refParity[f] = (best & 0x80000000ull) ? int8_t(-1) : int8_t(1);
-            refSplit[f] = static_cast<int>(best & 0x7FFFFFFFull);
-            atomicMin(&prm->winner, (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f));
+        if (lane == 0) {
+            // (error bits, featureIdx) of every candidate, for the runner-up report
+            candKey[c] = best != ~0ull ? (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f) : ~0ull;
+            if (best != ~0ull) {
+                refParity[f] = (best & 0x80000000ull) ? int8_t(-1) : int8_t(1);
+                refSplit[f] = static_cast<int>(best & 0x7FFFFFFFull);
+                atomicMin(&prm->winner, (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f));
+            }
         }
     }
 }
@@ -1047,6 +1052,7 @@ struct vj_trainer {
     float* d_wsg = nullptr;
     float* d_fastErr = nullptr;
     int* d_cand = nullptr;
+    unsigned long long* d_candKey = nullptr;
     int8_t* d_refParity = nullptr;
     int* d_refSplit = nullptr;
     RoundParams* d_prm = nullptr;
@@ -1063,11 +1069,13 @@ int ensure_round_scratch(vj_trainer* t) {
     cudaFree(t->d_wsg);
     cudaFree(t->d_fastErr);
     cudaFree(t->d_cand);
+    cudaFree(t->d_candKey);
     cudaFree(t->d_refParity);
     cudaFree(t->d_refSplit);
     t->d_wsg = nullptr;
     t->d_fastErr = nullptr;
     t->d_cand = nullptr;
+    t->d_candKey = nullptr;
     t->d_refParity = nullptr;
     t->d_refSplit = nullptr;
     t->scratchFeat = t->scratchN = 0;
@@ -1076,6 +1084,7 @@ int ensure_round_scratch(vj_trainer* t) {
     VJ_CUDA_TRY(cudaMalloc(&t->d_wsg, sizeof(float) * N));
     VJ_CUDA_TRY(cudaMalloc(&t->d_fastErr, sizeof(float) * F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_cand, sizeof(int) * F));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_candKey, sizeof(unsigned long long) * F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_refParity, F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_refSplit, sizeof(int) * F));
     if (!t->d_prm) VJ_CUDA_TRY(cudaMalloc(&t->d_prm, sizeof(RoundParams)));
@@ -1145,6 +1154,7 @@ int vj_trainer_destroy(vj_trainer* t) {
     cudaFree(t->d_wsg);
     cudaFree(t->d_fastErr);
     cudaFree(t->d_cand);
+    cudaFree(t->d_candKey);
     cudaFree(t->d_refParity);
     cudaFree(t->d_refSplit);
     cudaFree(t->d_prm);
@@ -1205,6 +1215,28 @@ int vj_trainer_last_round(vj_trainer* t, vj_round_info* out) {
     out->status = p.status;
     out->totalPos = p.tp;
     out->totalNeg = p.tn;
+    // the two smallest (error, featureIdx) keys among the exactly replayed candidates
+    out->bestFeature = out->runnerUpFeature = -1;
+    out->bestErr = out->runnerUpErr = INFINITY;
+    const int nc = static_cast<int>(std::min<int64_t>(p.ncand, t->scratchFeat));
+    if (nc > 0) {
+        std::vector<unsigned long long> keys(static_cast<size_t>(nc));
+        VJ_CUDA_TRY(cudaMemcpy(keys.data(), t->d_candKey, sizeof(unsigned long long) * keys.size(),
+                               cudaMemcpyDeviceToHost));
+        std::partial_sort(keys.begin(), keys.begin() + std::min(nc, 2), keys.end());
+        for (int k = 0; k < std::min(nc, 2); ++k) {
+            if (keys[static_cast<size_t>(k)] == ~0ull) break;
+            const float e = bits_float(static_cast<int32_t>(keys[static_cast<size_t>(k)] >> 32));
+            const int f = static_cast<int>(keys[static_cast<size_t>(k)] & 0xFFFFFFFFull);
+            if (k == 0) {
+                out->bestErr = e;
+                out->bestFeature = f;
+            } else {
+                out->runnerUpErr = e;
+                out->runnerUpFeature = f;
+            }
+        }
+    }
     return ok();
 }
 
@@ -1267,7 +1299,7 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_TIMED_LAUNCH("refine_kernel", s,
                         k<<<2 * sm_count(), kRefineThreads, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg,
                                                           n, t->d_prm, t->d_cand, t->d_refParity, t->d_refSplit,
-                                                          t->d_gate));
+                                                          t->d_candKey, t->d_gate));
         VJ_LAUNCH_CHECK("refine_kernel");
     }
     VJ_TIMED_LAUNCH("finalize_kernel", s,

@@ -296,8 +296,11 @@ int vj_trainer_prepare_stage(vj_trainer* t, void* stream);
 
 /* Statistics of the last vj_stump_search (no reference counterpart): the
  * fast-pass minimum error, the width of the candidate window, how many
- * features were replayed exactly, and the active weight totals.  Copies from
- * the device after synchronising the trainer's last stream. */
+ * features were replayed exactly, the active weight totals, and the two
+ * smallest exact (reference-replayed FP32) errors among the candidates - the
+ * pick and its runner-up (runnerUpFeature -1 and runnerUpErr +inf when the pick
+ * was the only candidate: every other feature's fast error exceeded the pick's
+ * by more than the window).  Copies from the device after synchronising. */
 typedef struct {
     float fastMin;
     float window;
@@ -305,6 +308,10 @@ typedef struct {
     int32_t status;  /* 0 ok, 1 no valid split in any feature */
     float totalPos;
     float totalNeg;
+    float bestErr;
+    int32_t bestFeature;
+    float runnerUpErr;
+    int32_t runnerUpFeature;
 } vj_round_info;
 
 int vj_trainer_last_round(vj_trainer* t, vj_round_info* out);

@@ -445,3 +445,33 @@ def test_stage_gate_queues_a_stage_without_reads(cuda, vj, oracle, basic_pool):
     assert (wb[k + 1:] == -1).all() and (cb[k + 1:] == 0).all()
     for x, y in zip(sb[0], sa[k]):
         assert np.array_equal(x, y)
+
+
+def test_last_round_reports_pick_and_runner_up(cuda, vj, oracle, gin, basic_pool):
+    """vj_trainer_last_round: the pick's exact error and feature equal the
+    search's output, and the runner-up among the exactly replayed candidates is
+    the oracle's second-best stump (the best of the pool with the pick masked),
+    up to features whose errors lie within the candidate window of it."""
+    patches = gin["ws_patches"]
+    labels = np.array([1] * 160 + [-1] * 160, np.int8)
+    rng = np.random.default_rng(12)
+    w = (rng.random(320) / 320).astype(np.float32)
+    feats = np.ascontiguousarray(basic_pool[:20000])
+    T = Train(cuda, vj, oracle, patches, labels, feats, w)
+    sums, inv = oracle.train_integrals(patches)
+    of = np.ascontiguousarray(feats).view(oracle.FEATURE)
+    for _ in range(3):
+        f, e, th, par = T.search(used=True)
+        info = T.t.lastRound()
+        assert info["bestFeature"] == f and np.float32(info["bestErr"]) == np.float32(e)
+        assert info["candidates"] >= 1 and info["status"] == 0
+        used = T.used.cpu().numpy().copy()
+        used[f] = 1
+        ru = oracle.weak_search(of, sums, inv, labels, T.w.cpu().numpy(), used=used, threads=8)
+        if info["runnerUpFeature"] >= 0:
+            assert info["runnerUpErr"] >= ru["err"] and info["runnerUpErr"] - ru["err"] <= info["window"]
+            if info["runnerUpErr"] == ru["err"]:
+                assert info["runnerUpFeature"] == ru["featureIdx"]
+        else:
+            assert ru["err"] > info["fastMin"]  # every other feature lay outside the window
+        assert T.t.applyBestWeak(T.best, T.strong, T.used) == 0
