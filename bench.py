@@ -510,9 +510,14 @@ def run_detect(V, torch, quick=False):
     t = time.perf_counter()
     O.detect(pool, st, sg, scene1080, norm_mode=0, threads=thr)
     cdt = time.perf_counter() - t
+    t = time.perf_counter()
+    O.detect(pool, st, sg, scene1080, norm_mode=0, threads=1)
+    cdt1 = time.perf_counter() - t
     out["cpu_baseline"] = {"value": 1.0 / cdt, "unit": "images/s", "cores": thr, "kind": "port",
                            "sample": "one 1920x1080 scene through the oracle's restatement of detectMultiScaleCpu "
-                                     f"(raw detections, no grouping), {cdt:.2f} s"}
+                                     f"(raw detections, no grouping), {cdt:.2f} s",
+                           "one_core": {"value": 1.0 / cdt1, "unit": "images/s", "cores": 1,
+                                        "sample": f"the same scene on one thread, {cdt1:.2f} s"}}
     return out
 
 
@@ -575,9 +580,14 @@ def cpu_baseline(pool, patches, target_s=15.0):
     nfeat = int(min(len(pool), max(nfeat, nfeat * target_s / max(dt, 1e-3))))
     dt = cpu_sample(pool, patches, nfeat, threads)
     gbs = BYTES_PER_ELEM_ROUND * nfeat * n / dt / 1e9
+    # the reference's CPU search is single-threaded: the same search on one core
+    n1 = max(8, int(nfeat * 3.0 / max(dt * threads, 1e-3)))
+    dt1 = cpu_sample(pool, patches, n1, 1)
     return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"one round of the oracle's restatement of runCpuWeakSearch over {nfeat} of 162,336 "
-                      f"features x {n} samples ({dt:.1f} s, {threads} threads), scaled by the 20 B model"}
+                      f"features x {n} samples ({dt:.1f} s, {threads} threads), scaled by the 20 B model",
+            "one_core": {"value": BYTES_PER_ELEM_ROUND * n1 * n / dt1 / 1e9, "unit": "GB/s", "cores": 1,
+                         "sample": f"{n1} features x {n} samples ({dt1:.1f} s, 1 thread)"}}
 
 
 def run_reference(args, rank, world):
