@@ -1169,8 +1169,12 @@ int vj_trainer_set_features(vj_trainer* t, const vj_haar_feature* features, int6
     for (int64_t i = 0; i < count; ++i) {
         const vj_haar_feature& f = features[i];
         const vj_fast_rect* rr[3] = {&f.r0, &f.r1, &f.r2};
-        if (f.tilted || (f.rectCount != 2 && f.rectCount != 3))
-            return set_error(VJ_INVALID_ARG, "vj_trainer_set_features: only upright 2/3-rect features train");
+        // Tilted features train like the reference trains them: their four
+        // corner indices are read from the upright integral like any others
+        // (the reference builds no tilted integral; IntegralImageSetT::d_tiltedT
+        // stays null, face_vision_engine.cu:1171).
+        if (f.rectCount != 2 && f.rectCount != 3)
+            return set_error(VJ_INVALID_ARG, "vj_trainer_set_features: features have 2 or 3 rectangles");
         for (int r = 0; r < f.rectCount; ++r) {
             const int32_t p[4] = {rr[r]->p0, rr[r]->p1, rr[r]->p2, rr[r]->p3};
             for (int c = 0; c < 4; ++c)

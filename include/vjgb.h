@@ -229,7 +229,9 @@ int vj_trainer_create(int winW, int winH, int maxSamples, vj_trainer** out);
 int vj_trainer_destroy(vj_trainer* t);
 
 /* FaceVisionEngine::uploadFeaturePool (face_vision_engine.cu:1022-1055) for
- * the training pool; host array, copied to the device. */
+ * the training pool; host array, copied to the device.  Tilted features are
+ * evaluated as the reference evaluates them: their four corner indices on the
+ * upright integral (the reference builds no tilted integral). */
 int vj_trainer_set_features(vj_trainer* t, const vj_haar_feature* features,
                             int64_t count);
 

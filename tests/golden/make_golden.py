@@ -3,7 +3,8 @@
 The reference (hengyizhu/CS677s26) ships no tests or golden vectors, so these
 are outputs of its CPU paths - buildHaarFeaturePool, buildHostIntegralImage,
 runCpuWeakSearch, resizeGrayBilinearHost, detectMultiScaleCpu,
-groupRectanglesCpu, cropResizeTo24 and ModelIO::saveCascadeModel - compiled from its sources
+groupRectanglesCpu, cropResizeTo24 and ModelIO::saveCascadeModel (also over tilted
+features) - compiled from its sources
 by oracle/Makefile into oracle/_ref/libvjref.so (only where the sources are,
 i.e. not on the GPU machines).  Inputs are seeded numpy arrays (stored in
 inputs.npz) or the package's synthetic generators (their bytes are hashed in
@@ -199,6 +200,45 @@ def main() -> None:
     inputs["crop_boxes"] = np.array(boxes, np.int32)
     inputs["crop_out"] = crops
     gold["crop"] = {"boxes": len(boxes), "out_sha256": sha(crops)}
+
+    # ---- tilted (All-mode) features: the reference evaluates their four corner
+    # indices on the upright integral like any other feature (it never builds a
+    # tilted integral); a weak search over them and a cascade that uses them
+    trng = np.random.default_rng(1677)
+    allp = O.feature_pool(2)
+    tidx = np.nonzero(allp["tilted"] == 1)[0]
+    gold["tilted_weak_search"] = []
+    for c, kind in enumerate(["uniform", "random"]):
+        idx = np.sort(trng.choice(tidx, 6000, replace=False))
+        w = (np.full(n, np.float32(0.5) / np.float32(160), np.float32) if kind == "uniform"
+             else (trng.random(n) / n).astype(np.float32))
+        r = ref_search(R, np.ascontiguousarray(allp[idx]), inputs["ws_patches"], labels, w)
+        key = f"tws_{c}"
+        inputs[key + "_idx"] = idx.astype(np.int32)
+        inputs[key + "_w"] = w
+        gold["tilted_weak_search"].append({"key": key, "kind": kind, **r})
+    # 3 stages x 10 tilted stumps, each stage threshold at the median stage sum
+    # of the windows that reach it (from the reference's own detection scores)
+    tst = np.zeros(30, dtype=V.STUMP4)
+    tst["featureBits"] = trng.choice(tidx, 30).astype(np.int32).view(np.float32)
+    tst["theta"] = trng.normal(0, 0.02, 30).astype(np.float32)
+    tst["leftVal"], tst["rightVal"] = -1.0, 1.0
+    tsg = np.zeros(3, dtype=V.STAGE)
+    tscene = V.synth_scene(150, 200, 150, 3, 24, 150)
+    cap = 200000
+    out = np.zeros(cap, O.DET)
+    for k in range(3):
+        tsg[k] = (10 * k, 10, np.float32(-1e30))
+        nd = R.ref_detect(allp.ctypes.data, len(allp), tst.ctypes.data, len(tst), tsg.ctypes.data, k + 1,
+                          tscene.ctypes.data, 200, 150, 200, 1.25, 24, cap, 0, out.ctypes.data, cap)
+        tsg[k]["threshold"] = np.float32(np.median(out[:nd]["score"]))
+    nd = R.ref_detect(allp.ctypes.data, len(allp), tst.ctypes.data, len(tst), tsg.ctypes.data, 3,
+                      tscene.ctypes.data, 200, 150, 200, 1.25, 24, cap, 0, out.ctypes.data, cap)
+    traw = out[:nd].copy()
+    g = np.zeros(max(1, nd), O.DET)
+    ng = R.ref_group(traw.ctypes.data, nd, 4, 0.2, g.ctypes.data, max(1, nd))
+    inputs.update(tdet_scene=tscene, tdet_stumps=tst, tdet_stages=tsg, tdet_raw=traw, tdet_grouped=g[:ng].copy())
+    gold["tilted_detect"] = {"raw": int(nd), "grouped": int(ng)}
 
     # ---- model file bytes
     with tempfile.TemporaryDirectory() as td:

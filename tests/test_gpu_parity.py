@@ -475,3 +475,25 @@ def test_last_round_reports_pick_and_runner_up(cuda, vj, oracle, gin, basic_pool
         else:
             assert ru["err"] > info["fastMin"]  # every other feature lay outside the window
         assert T.t.applyBestWeak(T.best, T.strong, T.used) == 0
+
+
+def test_tilted_features_like_the_reference(cuda, vj, oracle, golden, gin):
+    """The device search and detection over tilted (All-mode) features give the
+    reference's picks and raw detections (corner indices on the upright
+    integral, as the reference evaluates them), and the reference's clusters."""
+    allp = oracle.feature_pool(2)
+    patches = gin["ws_patches"]
+    labels = np.array([1] * 160 + [-1] * 160, np.int8)
+    for g in golden["tilted_weak_search"]:
+        T = Train(cuda, vj, oracle, patches, labels, np.ascontiguousarray(allp[gin[g["key"] + "_idx"]]),
+                  gin[g["key"] + "_w"])
+        assert T.search() == (g["featureIdx"], f32(g["err_bits"]), f32(g["theta_bits"]), g["parity"]), g
+    e = vj.FaceVisionEngine((24, 24), 1, 640, 480, False, 200000)
+    assert e.setCascadeModel(allp.view(vj.HAAR_FEATURE), gin["tdet_stumps"].view(vj.STUMP4),
+                             gin["tdet_stages"].view(vj.STAGE)) == 0
+    scene = gin["tdet_scene"]
+    s, raw = e.detectMultiScale(scene, 200, 150, 200, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0 and raw.tobytes() == gin["tdet_raw"].tobytes()
+    s, grp = e.detectMultiScale(scene, 200, 150, 200, 1.25, 4, 24, 200000)
+    assert s == 0 and as_set(grp) == as_set(gin["tdet_grouped"])
+    assert grp.tobytes() == oracle.group_first_order(raw, 4, 0.2).tobytes()

@@ -140,3 +140,21 @@ def test_crop_resize(oracle, golden, gin):
     assert len(boxes) == golden["crop"]["boxes"]
     for k, b in enumerate(boxes):
         assert np.array_equal(oracle.crop_resize(img, b).reshape(-1), out[k]), tuple(b)
+
+
+def test_tilted_features_like_the_reference(oracle, golden, gin):
+    """Tilted (All-mode) features: the reference evaluates their corner indices
+    on the upright integral; the oracle's search, detection and grouping over
+    them equal the reference's."""
+    allp = oracle.feature_pool(2)
+    patches = gin["ws_patches"]
+    sums, inv = oracle.train_integrals(patches)
+    labels = np.array([1] * 160 + [-1] * 160, np.int8)
+    for g in golden["tilted_weak_search"]:
+        feats = np.ascontiguousarray(allp[gin[g["key"] + "_idx"]])
+        b = oracle.weak_search(feats, sums, inv, labels, gin[g["key"] + "_w"])
+        assert b["featureIdx"] == g["featureIdx"]
+        assert b["err"] == f32(g["err_bits"]) and b["theta"] == f32(g["theta_bits"]) and b["parity"] == g["parity"]
+    raw = oracle.detect(allp, gin["tdet_stumps"], gin["tdet_stages"], gin["tdet_scene"], threads=8)
+    assert len(raw) == golden["tilted_detect"]["raw"] and raw.tobytes() == gin["tdet_raw"].tobytes()
+    assert oracle.group(raw, 4, 0.2).tobytes() == gin["tdet_grouped"].tobytes()
