@@ -953,8 +953,10 @@ __device__ __noinline__ int group_phases(const DevPlan& P, GridSync* G, unsigned
 //   3. tile pass (lane-per-window) over every level of every image;
 //   4. lane-per-window queue passes (optional);
 //   5. warp-per-window deep pass over the remaining stages;
-//   6. compaction of the raw detections, image after image, into the
-//      host-mapped buffer.
+//   6. layout of each image's kept raw detections (truncation key per image);
+//   7. with grouping, groupRectangles (group_phases);
+//   8. output: each image's clusters in order, or its raw detections, into
+//      the host-mapped buffer.
 // ---------------------------------------------------------------------------
 template <int TH, int MINB, int SL>
 __global__ void __launch_bounds__(kCasThreads, MINB)

@@ -517,10 +517,12 @@ int vj_detector_autotune(vj_detector* d, int n, const uint8_t* const* images,
 /* request that fits its share of the HBM budget (by                        */
 /* vj_detect_estimate_bytes) and runs them as one vj_detect_batch launch,   */
 /* so requests arriving while other batches are on the GPU join the next    */
-/* one (continuous batching).  Workers' launches share the GPU: each uses   */
-/* blocksPerSM CTAs per SM (0 = the SM's capacity split evenly among the    */
-/* workers), so two batches run on the device at once.  Every result equals */
-/* vj_detect on that image alone.                                           */
+/* one (continuous batching).  With blocksPerSM 0 each worker's kernel      */
+/* fills the GPU and the workers' kernels take turns on the device (one     */
+/* worker's planning, uploads and copies overlap another's kernel); a       */
+/* smaller blocksPerSM splits the SMs and lets batches run side by side.    */
+/* maxBatchPixels caps a batch's work.  Every result equals vj_detect on    */
+/* that image alone.                                                        */
 /* ------------------------------------------------------------------------ */
 
 typedef struct vj_server vj_server;
