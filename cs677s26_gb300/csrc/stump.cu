@@ -477,7 +477,8 @@ __global__ void __launch_bounds__(kRefineThreads)
 refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
               int64_t gapStride, const float* __restrict__ wsgG, int n, RoundParams* __restrict__ prm,
               const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit,
-              unsigned long long* __restrict__ candKey, const int* gate) {
+              unsigned long long* __restrict__ candKey, float2* __restrict__ prefix, int64_t prefixStride,
+              const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ float wsgS[];
     __shared__ __align__(16) float stage[kRefineWarps][256];   // gathered weights of one chunk, in order
@@ -489,6 +490,7 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
         wsg = wsgS;
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kRefineWarps + w;  // row of `prefix` this warp uses
     const int nc = prm->ncand;
     // One warp per candidate feature.  The warp streams the feature's sorted
     // order 256 positions at a time (one coalesced 16-byte load per lane,
@@ -519,7 +521,11 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
             st[0] = make_float4(x[0], x[1], x[2], x[3]);
             st[1] = make_float4(x[4], x[5], x[6], x[7]);
         };
-        // Pass 1: totals over all positions in sorted order.
+        // One sequential pass (lane 0): the left sums after every position, in
+        // sorted order, into the warp's row of `prefix`.  Carried on to the last
+        // position, the same chain gives the totals: the reference adds the
+        // same weights in the same order for both (main.cu:626-645).
+        float2* prow = prefix + static_cast<size_t>(gw) * prefixStride;
         float tp = 0.0f, tn = 0.0f;
         {
             uint4 v = load(0);
@@ -539,63 +545,43 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
                             const float a = fabsf(e[h]);
                             tp = __fadd_rn(tp, neg ? 0.0f : a);
                             tn = __fadd_rn(tn, neg ? a : 0.0f);
+                            pre[w][4 * j + h] = make_float2(tp, tn);
                         }
                     }
                 }
+                __syncwarp();
+                // the chunk's left sums to the warp's row, all lanes, coalesced
+                const int lim = min(256, n - 1 - base);  // positions scored: 0 .. n-2
+                for (int q = lane; q < lim; q += 32) prow[base + q] = pre[w][q];
                 __syncwarp();
                 v = vn;
             }
         }
         tp = __shfl_sync(0xffffffffu, tp, 0);
         tn = __shfl_sync(0xffffffffu, tn, 0);
-        // Pass 2: left sums after each position (lane 0), then every lane
-        // scores its 8 positions.  The reference's update rule over the
-        // candidates in split order (lower error replaces; at equal error
-        // parity +1 replaces parity -1) picks the lexicographic minimum of
-        // (error, parity +1 before -1, split index); errors are >= +0, so the
-        // float bits order like the values and the triple packs into one key.
+        __syncwarp();
+        // Scoring, every lane over its positions.  The reference's update rule
+        // over the candidates in split order (lower error replaces; at equal
+        // error parity +1 replaces parity -1) picks the lexicographic minimum
+        // of (error, parity +1 before -1, split index); errors are >= +0, so
+        // the float bits order like the values and the triple packs into one
+        // key.
         unsigned long long best = ~0ull;
-        {
-            float lp = 0.0f, ln = 0.0f;
-            uint4 v = load(0);
-            for (int base = 0; base < n - 1; base += 256) {
-                const uint4 vn = load(base + 256);
-                gather(base, v);
-                __syncwarp();
-                if (lane == 0) {
-                    const float4* st = reinterpret_cast<const float4*>(stage[w]);
-#pragma unroll 4
-                    for (int j = 0; j < 64; ++j) {
-                        const float4 q = st[j];
-                        const float e[4] = {q.x, q.y, q.z, q.w};
+        for (int base = 0; base < n - 1; base += 256) {
+            const int k0 = base + lane * 8;
+            const uint32_t g = (k0 < n - 1) ? (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu : 0u;
 #pragma unroll
-                        for (int h = 0; h < 4; ++h) {
-                            const bool neg = signbit(e[h]);
-                            const float a = fabsf(e[h]);
-                            lp = __fadd_rn(lp, neg ? 0.0f : a);
-                            ln = __fadd_rn(ln, neg ? a : 0.0f);
-                            pre[w][4 * j + h] = make_float2(lp, ln);
-                        }
-                    }
+            for (int h = 0; h < 8; ++h) {
+                if ((g >> h) & 1u) {
+                    const float2 l = prow[k0 + h];
+                    const float eL = __fadd_rn(l.y, __fsub_rn(tp, l.x));  // parity -1
+                    const float eR = __fadd_rn(l.x, __fsub_rn(tn, l.y));  // parity +1
+                    const unsigned k = static_cast<unsigned>(k0 + h);
+                    const unsigned long long kL =
+                        (static_cast<unsigned long long>(__float_as_uint(eL)) << 32) | 0x80000000u | k;
+                    const unsigned long long kR = (static_cast<unsigned long long>(__float_as_uint(eR)) << 32) | k;
+                    best = min(best, min(kL, kR));
                 }
-                __syncwarp();
-                const int k0 = base + lane * 8;
-                const uint32_t g = (k0 < n - 1) ? (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu : 0u;
-#pragma unroll
-                for (int h = 0; h < 8; ++h) {
-                    if ((g >> h) & 1u) {
-                        const float2 l = pre[w][lane * 8 + h];
-                        const float eL = __fadd_rn(l.y, __fsub_rn(tp, l.x));  // parity -1
-                        const float eR = __fadd_rn(l.x, __fsub_rn(tn, l.y));  // parity +1
-                        const unsigned k = static_cast<unsigned>(k0 + h);
-                        const unsigned long long kL =
-                            (static_cast<unsigned long long>(__float_as_uint(eL)) << 32) | 0x80000000u | k;
-                        const unsigned long long kR = (static_cast<unsigned long long>(__float_as_uint(eR)) << 32) | k;
-                        best = min(best, min(kL, kR));
-                    }
-                }
-                __syncwarp();
-                v = vn;
             }
         }
 #pragma unroll
@@ -652,23 +638,34 @@ __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const
 // partial sums are combined by a fixed halving tree, so the result does not
 // depend on scheduling.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024)
+// Round update in two kernels with the arithmetic of one 1024-thread block:
+// thread t of 1024 (kRoundUpdateCtas blocks of 256) accumulates, in double and
+// in sample order, the new unnormalised weights of samples t, t+1024, ...
+// (partial t); the normaliser Z is the halving-tree sum of the 1024 partials,
+// and every weight is divided by Z in double.  The second kernel spreads the
+// divisions (FP64, the round's costliest part) over many blocks; each block
+// rebuilds Z from the partials in the same tree order.
+constexpr int kRoundUpdateCtas = 4;
+constexpr int kRoundPartials = 1024;
+
+__device__ __forceinline__ bool best_valid(const vj_tile_best& b) { return b.featureIdx >= 0 && isfinite(b.bestErr); }
+
+__global__ void __launch_bounds__(256)
 round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_best* __restrict__ best,
                     const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm,
                     const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
-                    float* __restrict__ weight, float* __restrict__ strong, int n,
+                    const float* __restrict__ weight, float* __restrict__ strong, int n,
                     uint8_t* __restrict__ usedMask, vj_weak_classifier* __restrict__ weakOut,
-                    int* __restrict__ status, int* gate) {
+                    int* __restrict__ status, double* __restrict__ xbuf, double* __restrict__ partials, int* gate) {
     if (gate_closed(gate)) return;
-    __shared__ double part[1024];
     __shared__ vj_haar_feature sfeat;
     __shared__ float sTheta, sLeft, sRight;
     __shared__ double sF;
     __shared__ int sPar, sValid;
-    const int tid = threadIdx.x;
-    if (tid == 0) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;  // partial index, 0..1023
+    if (threadIdx.x == 0) {
         const vj_tile_best b = *best;
-        const bool valid = b.featureIdx >= 0 && isfinite(b.bestErr);
+        const bool valid = best_valid(b);
         sValid = valid ? 1 : 0;
         if (valid) {
             const float eps = 1e-6f;
@@ -681,22 +678,26 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
             sLeft = b.bestParity > 0 ? -C : C;
             sRight = b.bestParity > 0 ? C : -C;
             sfeat = feats[b.featureIdx];
-            if (weakOut) {
-                vj_weak_classifier wc;
-                wc.featureIdx = b.featureIdx;
-                wc.theta = b.bestTheta;
-                wc.parity = b.bestParity;
-                wc.pad0 = wc.pad1 = wc.pad2 = 0;
-                wc.err = e;
-                wc.alpha = C;
-                wc.leftVal = sLeft;
-                wc.rightVal = sRight;
-                *weakOut = wc;
+            if (blockIdx.x == 0) {
+                if (weakOut) {
+                    vj_weak_classifier wc;
+                    wc.featureIdx = b.featureIdx;
+                    wc.theta = b.bestTheta;
+                    wc.parity = b.bestParity;
+                    wc.pad0 = wc.pad1 = wc.pad2 = 0;
+                    wc.err = e;
+                    wc.alpha = C;
+                    wc.leftVal = sLeft;
+                    wc.rightVal = sRight;
+                    *weakOut = wc;
+                }
+                if (usedMask) usedMask[b.featureIdx] = 1;
             }
-            if (usedMask) usedMask[b.featureIdx] = 1;
         }
-        if (status) *status = valid ? 0 : 1;
-        if (!valid && gate) *gate = 2;
+        if (blockIdx.x == 0) {
+            if (status) *status = valid ? 0 : 1;
+            if (!valid && gate) *gate = 2;
+        }
     }
     __syncthreads();
     if (!sValid) return;
@@ -704,37 +705,40 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
     const float theta = sTheta, left = sLeft, right = sRight;
     const double F = sF;
     const int par = sPar;
-    uint64_t mis = 0;  // n <= 65535 -> at most 64 samples per thread
     double acc = 0.0;
-    for (int i = tid, j = 0; i < n; i += 1024, ++j) {
+    for (int i = t; i < n; i += kRoundPartials) {
         const float r = train_response(f, sumT, n, i, invNorm[i]);
         const bool lt = r < theta;
         strong[i] = __fadd_rn(strong[i], lt ? left : right);
         const bool act = active == nullptr || active[i] != 0;
-        if (!act) continue;
-        const int pred = par > 0 ? (lt ? -1 : 1) : (lt ? 1 : -1);
-        const bool m = pred != static_cast<int>(label[i]);
-        double x = static_cast<double>(weight[i]);
-        if (m) {
-            mis |= 1ull << j;
-            x = x * F;
+        if (!act) {
+            xbuf[i] = 0.0;
+            continue;
         }
+        const int pred = par > 0 ? (lt ? -1 : 1) : (lt ? 1 : -1);
+        double x = static_cast<double>(weight[i]);
+        if (pred != static_cast<int>(label[i])) x = x * F;
+        xbuf[i] = x;
         acc += x;
     }
-    part[tid] = acc;
+    partials[t] = acc;
+}
+
+__global__ void __launch_bounds__(256)
+round_normalize_kernel(const vj_tile_best* __restrict__ best, const double* __restrict__ xbuf,
+                       const double* __restrict__ partials, float* __restrict__ weight, int n, const int* gate) {
+    if (gate_closed(gate)) return;
+    if (!best_valid(*best)) return;
+    __shared__ double part[kRoundPartials];
+    for (int k = threadIdx.x; k < kRoundPartials; k += blockDim.x) part[k] = partials[k];
     __syncthreads();
-    for (int s = 512; s >= 1; s >>= 1) {
-        if (tid < s) part[tid] = part[tid] + part[tid + s];
+    for (int s = kRoundPartials / 2; s >= 1; s >>= 1) {
+        for (int k = threadIdx.x; k < s; k += blockDim.x) part[k] = part[k] + part[k + s];
         __syncthreads();
     }
     const double Z = part[0];
-    for (int i = tid, j = 0; i < n; i += 1024, ++j) {
-        const bool act = active == nullptr || active[i] != 0;
-        double x = 0.0;
-        if (act) {
-            x = static_cast<double>(weight[i]);
-            if ((mis >> j) & 1ull) x = x * F;
-        }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double x = xbuf[i];
         weight[i] = (Z > 1e-30) ? static_cast<float>(x / Z) : static_cast<float>(x);
     }
 }
@@ -999,6 +1003,9 @@ int sm_count() {
     return cached;
 }
 
+// Blocks of the refine launch: one per SM (each warp takes candidates in turn).
+int refine_blocks() { return sm_count(); }
+
 // Launches eval_sort_kernel with the smallest items-per-thread that holds n.
 int launch_eval_sort(const vj_haar_feature* feats, int featBegin, int featCount, const uint32_t* sumT,
                      const float* invNorm, int n, const float* resp, uint16_t* ordOut, int64_t ordStride,
@@ -1053,6 +1060,9 @@ struct vj_trainer {
     float* d_fastErr = nullptr;
     int* d_cand = nullptr;
     unsigned long long* d_candKey = nullptr;
+    double* d_xbuf = nullptr;      // unnormalised new weights of the round update
+    double* d_partials = nullptr;  // its 1024 partial sums
+    float2* d_prefix = nullptr;    // refine: left sums after each position, one row per warp
     int8_t* d_refParity = nullptr;
     int* d_refSplit = nullptr;
     RoundParams* d_prm = nullptr;
@@ -1070,12 +1080,18 @@ int ensure_round_scratch(vj_trainer* t) {
     cudaFree(t->d_fastErr);
     cudaFree(t->d_cand);
     cudaFree(t->d_candKey);
+    cudaFree(t->d_xbuf);
+    cudaFree(t->d_partials);
+    cudaFree(t->d_prefix);
     cudaFree(t->d_refParity);
     cudaFree(t->d_refSplit);
     t->d_wsg = nullptr;
     t->d_fastErr = nullptr;
     t->d_cand = nullptr;
     t->d_candKey = nullptr;
+    t->d_xbuf = nullptr;
+    t->d_partials = nullptr;
+    t->d_prefix = nullptr;
     t->d_refParity = nullptr;
     t->d_refSplit = nullptr;
     t->scratchFeat = t->scratchN = 0;
@@ -1085,6 +1101,9 @@ int ensure_round_scratch(vj_trainer* t) {
     VJ_CUDA_TRY(cudaMalloc(&t->d_fastErr, sizeof(float) * F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_cand, sizeof(int) * F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_candKey, sizeof(unsigned long long) * F));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_xbuf, sizeof(double) * N));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_partials, sizeof(double) * kRoundPartials));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_prefix, sizeof(float2) * static_cast<size_t>(refine_blocks()) * kRefineWarps * N));
     VJ_CUDA_TRY(cudaMalloc(&t->d_refParity, F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_refSplit, sizeof(int) * F));
     if (!t->d_prm) VJ_CUDA_TRY(cudaMalloc(&t->d_prm, sizeof(RoundParams)));
@@ -1155,6 +1174,9 @@ int vj_trainer_destroy(vj_trainer* t) {
     cudaFree(t->d_fastErr);
     cudaFree(t->d_cand);
     cudaFree(t->d_candKey);
+    cudaFree(t->d_xbuf);
+    cudaFree(t->d_partials);
+    cudaFree(t->d_prefix);
     cudaFree(t->d_refParity);
     cudaFree(t->d_refSplit);
     cudaFree(t->d_prm);
@@ -1301,9 +1323,10 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         auto k = smemW ? refine_kernel<true> : refine_kernel<false>;
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("refine_kernel", s,
-                        k<<<2 * sm_count(), kRefineThreads, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg,
-                                                          n, t->d_prm, t->d_cand, t->d_refParity, t->d_refSplit,
-                                                          t->d_candKey, t->d_gate));
+                        k<<<refine_blocks(), kRefineThreads, wbytes, s>>>(
+                            t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, t->d_prm, t->d_cand,
+                            t->d_refParity, t->d_refSplit, t->d_candKey, t->d_prefix, static_cast<int64_t>(t->maxSamples),
+                            t->d_gate));
         VJ_LAUNCH_CHECK("refine_kernel");
     }
     VJ_TIMED_LAUNCH("finalize_kernel", s,
@@ -1322,10 +1345,14 @@ int vj_round_update(vj_trainer* t, const vj_tile_best* d_best, float* d_strong, 
     if (st != VJ_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VJ_TIMED_LAUNCH("round_update_kernel", s,
-                    round_update_kernel<<<1, 1024, 0, s>>>(t->d_feat, d_best, t->d_sumT, t->d_invNorm, t->d_label,
-                                                           t->d_active, t->d_weight, d_strong, t->n, d_usedMask,
-                                                           d_weak_out, t->d_status, t->d_gate));
+                    round_update_kernel<<<kRoundUpdateCtas, 256, 0, s>>>(
+                        t->d_feat, d_best, t->d_sumT, t->d_invNorm, t->d_label, t->d_active, t->d_weight, d_strong,
+                        t->n, d_usedMask, d_weak_out, t->d_status, t->d_xbuf, t->d_partials, t->d_gate));
     VJ_LAUNCH_CHECK("round_update_kernel");
+    VJ_TIMED_LAUNCH("round_normalize_kernel", s,
+                    round_normalize_kernel<<<std::min(div_up(t->n, 256), 2 * sm_count()), 256, 0, s>>>(
+                        d_best, t->d_xbuf, t->d_partials, t->d_weight, t->n, t->d_gate));
+    VJ_LAUNCH_CHECK("round_normalize_kernel");
     return ok();
 }
 
