@@ -631,19 +631,21 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
 //
 // Per-warp shared memory: 32 floats of values, then SL patches.
 // ---------------------------------------------------------------------------
+constexpr int kDeepEvals = 3;  // stumps a lane evaluates per step
 __host__ __device__ constexpr int deep_warp_floats(int slots, int patchElems) {
-    return 32 + ((slots * patchElems + 3) & ~3);
+    return 32 * kDeepEvals + ((slots * patchElems + 3) & ~3);
 }
 
 template <int SL>
 __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QEntry* q, int n,
                                           unsigned long long* workCounter, unsigned long long& evals) {
-    constexpr int LPS = 32 / SL;  // lanes per slot
+    constexpr int LPS = 32 / SL;           // lanes per slot
+    constexpr int SPS = LPS * kDeepEvals;  // stumps per slot per step
     const int lane = threadIdx.x & 31;
     const int slot = lane / LPS, j = lane % LPS;
     const int pw = P.winW + 1, ph = P.winH + 1, pe = pw * ph;
-    float* vals = wsm;
-    float* patches = wsm + 32;
+    float* vals = wsm;  // per slot SPS values in stump order
+    float* patches = wsm + 32 * kDeepEvals;
     const float* myPatch = patches + slot * pe;
     int qi = -1;  // queue index of the slot's window, -1 = empty
     QEntry e{};
@@ -694,15 +696,18 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
         const bool active = qi >= 0;
         DStage st{0, 0, 0.0f, 0};
         if (active) st = P.stages[si];
-        const int k = k0 + j;
-        float c = 0.0f;
-        if (active && k < st.ntrees) c = patch_stump_value(P.pstumps, st.first + k, myPatch, e.inv);
-        vals[lane] = c;
-        __syncwarp();
-        const int m = active ? min(LPS, st.ntrees - k0) : 0;
-        const float4* v4 = reinterpret_cast<const float4*>(vals + slot * LPS);
 #pragma unroll
-        for (int g = 0; g < LPS / 4; ++g) {
+        for (int ev = 0; ev < kDeepEvals; ++ev) {
+            const int k = k0 + ev * LPS + j;
+            float c = 0.0f;
+            if (active && k < st.ntrees) c = patch_stump_value(P.pstumps, st.first + k, myPatch, e.inv);
+            vals[slot * SPS + ev * LPS + j] = c;
+        }
+        __syncwarp();
+        const int m = active ? min(SPS, st.ntrees - k0) : 0;
+        const float4* v4 = reinterpret_cast<const float4*>(vals + slot * SPS);
+#pragma unroll
+        for (int g = 0; g < SPS / 4; ++g) {
             const float4 x = v4[g];
             if (4 * g + 0 < m) acc = __fadd_rn(acc, x.x);
             if (4 * g + 1 < m) acc = __fadd_rn(acc, x.y);
@@ -711,7 +716,7 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
         }
         __syncwarp();
         if (j == 0) evals += static_cast<unsigned>(m);
-        k0 += LPS;
+        k0 += SPS;
         if (active && k0 >= st.ntrees) {
             if (acc < st.threshold) {
                 qi = -1;
