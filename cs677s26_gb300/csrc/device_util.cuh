@@ -32,6 +32,11 @@ __device__ __forceinline__ uint32_t radix_key(uint32_t bits) {
     return bits ^ (static_cast<uint32_t>(static_cast<int32_t>(bits) >> 31) | 0x80000000u);
 }
 
+// Inverse of radix_key: the float bits back from the order-preserving key.
+__device__ __forceinline__ uint32_t radix_key_inv(uint32_t key) {
+    return key ^ (static_cast<uint32_t>(static_cast<int32_t>(key ^ 0x80000000u) >> 31) | 0x80000000u);
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

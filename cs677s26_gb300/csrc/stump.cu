@@ -61,6 +61,19 @@ __device__ __forceinline__ bool gate_closed(const int* g) {
     return g != nullptr && *reinterpret_cast<const volatile int*>(g) != 0;
 }
 
+// Resident stage orders (one row per feature) are stored chunk-interleaved:
+// in each chunk of 512 sorted positions, positions 16l..16l+7 sit at slots
+// 8l..8l+7 and positions 16l+8..16l+15 at slots 256+8l..256+8l+7.  A sweep
+// lane owns the 16 consecutive positions 16l..16l+15 of a chunk, and with
+// this layout each of its two 16-byte loads is contiguous across the warp
+// (512 B per load instruction instead of 1 KB half-used).  Any 8 consecutive
+// positions starting at a multiple of 8 stay contiguous.  Rows are padded to
+// a multiple of 512 positions.
+__host__ __device__ __forceinline__ int64_t ord_slot(int64_t k) {
+    const int64_t r = k & 511;
+    return (k - r) + ((r >> 3) & 1) * 256 + (r >> 4) * 8 + (r & 7);
+}
+
 struct RoundParams {
     float tp, tn, w;             // active positive / negative weight and their sum
     float window;                // candidate window above the fast minimum
@@ -74,9 +87,16 @@ struct RoundParams {
 // ---------------------------------------------------------------------------
 // 1. Evaluate + on-chip stable radix sort of one feature per CTA.
 // ---------------------------------------------------------------------------
+// Up to 24 items per thread the sort ping-pongs two index buffers in shared
+// memory, so an item's sample index is re-read from the source buffer when it
+// is scattered and only its 16-bit rank and 8-bit digit stay in registers;
+// 32 items per thread keep the indices in registers (one buffer).
+template <int R>
+__host__ __device__ constexpr bool sort_ping_pong() { return R <= 24; }
+
 template <int R>
 constexpr size_t sort_smem_bytes() {
-    return static_cast<size_t>(1024 * R) * (4 + 2) + 256 * kCntStride * 4;
+    return static_cast<size_t>(1024 * R) * (4 + (sort_ping_pong<R>() ? 4 : 2)) + 256 * kCntStride * 4;
 }
 
 template <int R, bool kFromResp>
@@ -86,10 +106,12 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                  const float* __restrict__ resp, uint16_t* __restrict__ ordOut, int64_t ordStride,
                  bool ordPadded, uint32_t* __restrict__ gapOut, int64_t gapStride) {
     constexpr int NP = 1024 * R;
+    constexpr bool kPP = sort_ping_pong<R>();
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);  // float bits in sample order
-    uint16_t* idx = reinterpret_cast<uint16_t*>(keys + NP);
-    uint32_t* cnt = reinterpret_cast<uint32_t*>(idx + NP);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);  // radix keys of the responses, in sample order
+    uint16_t* idx = reinterpret_cast<uint16_t*>(keys + NP);   // sorted order after the last pass
+    uint16_t* idx2 = idx + NP;                                // second buffer (kPP only)
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(idx + (kPP ? 2 * NP : NP));
     __shared__ uint32_t warpTot[32];
     __shared__ vj_haar_feature sfeat;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -98,7 +120,7 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
     for (int fl = blockIdx.x; fl < featCount; fl += gridDim.x) {
         if (kFromResp) {
             const float* row = resp + static_cast<size_t>(fl) * n;
-            for (int s = tid; s < n; s += kSortThreads) keys[s] = __float_as_uint(row[s]);
+            for (int s = tid; s < n; s += kSortThreads) keys[s] = radix_key(__float_as_uint(row[s]));
         } else {
             if (tid == 0) sfeat = feats[featBegin + fl];
             __syncthreads();
@@ -113,7 +135,7 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                 }
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    if (s0 + u * kSortThreads < n) keys[s0 + u * kSortThreads] = __float_as_uint(r[u]);
+                    if (s0 + u * kSortThreads < n) keys[s0 + u * kSortThreads] = radix_key(__float_as_uint(r[u]));
             }
         }
         for (int p = tid; p < NP; p += kSortThreads) idx[p] = static_cast<uint16_t>(p);
@@ -121,6 +143,9 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
 
         for (int pass = 0; pass < 4; ++pass) {
             const int shift = pass * 8;
+            // with two buffers, even passes read idx and write idx2, odd ones the reverse
+            const uint16_t* src = (kPP && (pass & 1)) ? idx2 : idx;
+            uint16_t* dst = (kPP && !(pass & 1)) ? idx2 : idx;
             for (int i = tid; i < 256 * kCntStride; i += kSortThreads) cnt[i] = 0;
             __syncthreads();
             // Rank every item among equal digits: items are warp-striped, so
@@ -129,14 +154,20 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
             // counter for that digit.
             // Digits first (independent loads), then ranks: peers with the
             // same digit in a step come from 8 ballots, one per digit bit.
-            uint32_t packed[R];
+            // packed[j]: the item's sample index in the low half (one buffer
+            // only) and its rank among equal digits in the high half; with
+            // two buffers, items j and j+1 share a word of two 16-bit ranks.
+            constexpr int kPacked = kPP ? (R + 1) / 2 : R;
+            uint32_t packed[kPacked];
             uint32_t dig[(R + 3) / 4];
+#pragma unroll
+            for (int j = 0; j < kPacked; ++j) packed[j] = 0;
 #pragma unroll
             for (int j = 0; j < R; ++j) {
                 const int p = warp * 32 * R + j * 32 + lane;
-                const uint32_t id = idx[p];
-                const uint32_t d = id < static_cast<uint32_t>(n) ? (radix_key(keys[id]) >> shift) & 255u : 255u;
-                packed[j] = id;
+                const uint32_t id = src[p];
+                const uint32_t d = id < static_cast<uint32_t>(n) ? (keys[id] >> shift) & 255u : 255u;
+                if (!kPP) packed[j] = id;
                 if ((j & 3) == 0)
                     dig[j >> 2] = d;
                 else
@@ -158,7 +189,11 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                     cnt[d * kCntStride + warp] = old + __popc(peers);
                 }
                 old = __shfl_sync(0xffffffffu, old, leader);
-                packed[j] |= (old + __popc(peers & lanemask_lt())) << 16;
+                const uint32_t rank = old + __popc(peers & lanemask_lt());
+                if (kPP)
+                    packed[j >> 1] |= rank << (16 * (j & 1));
+                else
+                    packed[j] |= rank << 16;
             }
             __syncthreads();
             // Exclusive scan of the counters in (digit, warp) order.
@@ -199,36 +234,38 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
 #pragma unroll
             for (int j = 0; j < R; ++j) {
                 const uint32_t d = (dig[j >> 2] >> (8 * (j & 3))) & 255u;
-                const uint32_t pos = cnt[d * kCntStride + warp] + (packed[j] >> 16);
-                idx[pos] = static_cast<uint16_t>(packed[j] & 0xFFFFu);
+                if (kPP) {
+                    const uint32_t rank = (packed[j >> 1] >> (16 * (j & 1))) & 0xFFFFu;
+                    dst[cnt[d * kCntStride + warp] + rank] = src[warp * 32 * R + j * 32 + lane];
+                } else {
+                    const uint32_t pos = cnt[d * kCntStride + warp] + (packed[j] >> 16);
+                    idx[pos] = static_cast<uint16_t>(packed[j] & 0xFFFFu);
+                }
             }
             __syncthreads();
         }
 
-        // Sorted sample order.
+        // Sorted sample order (padded rows: chunk-interleaved, see ord_slot).
         uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
         if (ordPadded) {
             const int n8 = (n + 7) & ~7;
             for (int k = tid * 8; k < n8; k += kSortThreads * 8)
-                *reinterpret_cast<uint4*>(orow + k) = *reinterpret_cast<const uint4*>(idx + k);
+                *reinterpret_cast<uint4*>(orow + ord_slot(k)) = *reinterpret_cast<const uint4*>(idx + k);
         } else {
             for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
         }
         // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
+        // A warp takes 32 consecutive positions per step, one per lane; the
+        // next value comes from the next lane, and the word from one ballot.
         if (gapOut) {
             uint32_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
-            for (int wd = tid; wd < gapWords; wd += kSortThreads) {
-                uint32_t bits = 0;
-                const int k0 = wd * 32;
-                float v0 = __uint_as_float(keys[idx[k0]]);
-                for (int b = 0; b < 32; ++b) {
-                    const int k = k0 + b;
-                    if (k + 1 >= n) break;
-                    const float v1 = __uint_as_float(keys[idx[k + 1]]);
-                    if (__fadd_rn(v0, 1e-7f) < v1) bits |= 1u << b;
-                    v0 = v1;
-                }
-                grow[wd] = bits;
+            for (int k0 = warp * 32; k0 < gapWords * 32; k0 += kSortThreads) {
+                const int k = k0 + lane;
+                const float v0 = k < n ? __uint_as_float(radix_key_inv(keys[idx[k]])) : 0.0f;
+                float v1 = __shfl_down_sync(0xffffffffu, v0, 1);
+                if (lane == 31 && k + 1 < n) v1 = __uint_as_float(radix_key_inv(keys[idx[k + 1]]));
+                const uint32_t bits = __ballot_sync(0xffffffffu, k + 1 < n && __fadd_rn(v0, 1e-7f) < v1);
+                if (lane == 0) grow[k0 >> 5] = bits;
             }
         }
         __syncthreads();
@@ -348,9 +385,9 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t
         g = 0;
         if (it >= items) return;
         const int k0 = c * 512 + lane * 16;
-        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
-        if (k0 < n) a = __ldg(reinterpret_cast<const uint4*>(row + k0));
-        if (k0 + 8 < n) b = __ldg(reinterpret_cast<const uint4*>(row + k0 + 8));
+        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride + c * 512 + lane * 8;  // ord_slot(k0)
+        if (k0 < n) a = __ldg(reinterpret_cast<const uint4*>(row));
+        if (k0 + 8 < n) b = __ldg(reinterpret_cast<const uint4*>(row + 256));
         if (k0 < n - 1) g = (__ldg(gap + static_cast<size_t>(f) * gapStride + (k0 >> 5)) >> (k0 & 31)) & 0xFFFFu;
     };
     float blockMin = INFINITY;
@@ -505,7 +542,7 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
         const uint32_t* grow = gap + static_cast<size_t>(f) * gapStride;
         auto load = [&](int base) {
             const int k0 = base + lane * 8;
-            return (k0 < n) ? __ldg(reinterpret_cast<const uint4*>(row + k0)) : make_uint4(0, 0, 0, 0);
+            return (k0 < n) ? __ldg(reinterpret_cast<const uint4*>(row + ord_slot(k0))) : make_uint4(0, 0, 0, 0);
         };
         auto gather = [&](int base, const uint4& v) {
             const int k0 = base + lane * 8;
@@ -619,7 +656,7 @@ __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const
         const int f = static_cast<int>(w & 0xFFFFFFFFull);
         const int k = refSplit[f];
         const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
-        const int s0 = row[k], s1 = row[k + 1];
+        const int s0 = row[ord_slot(k)], s1 = row[ord_slot(k + 1)];
         const vj_haar_feature ft = feats[f];
         const float v0 = train_response(ft, sumT, n, s0, invNorm[s0]);
         const float v1 = train_response(ft, sumT, n, s1, invNorm[s1]);
@@ -1122,7 +1159,7 @@ int check_bound(vj_trainer* t, const char* fn) {
 
 // Writes the per-feature orders and split masks for the whole pool.
 int sort_all(vj_trainer* t, cudaStream_t s) {
-    const int64_t ordStride = (t->n + 7) & ~7;
+    const int64_t ordStride = (static_cast<int64_t>(t->n) + 511) & ~int64_t(511);  // whole 512-position chunks
     const int64_t gapStride = (t->n + 31) / 32;
     const size_t ordBytes = static_cast<size_t>(t->nFeat) * ordStride * sizeof(uint16_t);
     const size_t gapBytes = static_cast<size_t>(t->nFeat) * gapStride * sizeof(uint32_t);
