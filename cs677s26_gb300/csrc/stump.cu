@@ -13,7 +13,9 @@
 //      responses of all samples into shared memory and sorts them with an
 //      on-chip stable LSD radix sort (4 x 8-bit digits, ranks from warp
 //      ballots, per-warp digit counters).  It writes the sorted sample order (2 B per
-//      feature-sample) and a bitmask of valid split positions
+//      feature-sample: the sample index, or for up to kTwoCopyMax samples the
+//      shared-memory slot of one of two weight copies, chosen against bank
+//      conflicts in the sweep) and a bitmask of valid split positions
 //      (v[k] + 1e-7f < v[k+1], boosting_core.cu:400).
 //   2. sweep_kernel: one warp per feature streams that order, gathers signed
 //      weights from shared memory and forms FP32 prefix sums (8-element lane
@@ -74,6 +76,37 @@ __host__ __device__ __forceinline__ int64_t ord_slot(int64_t k) {
     return (k - r) + ((r >> 3) & 1) * 256 + (r >> 4) * 8 + (r & 7);
 }
 
+// Two copies of the round's signed weights in shared memory (n <= kTwoCopyMax):
+// copy 0 at [0, n), copy 1 at base + copy1_offset(i) with base = n rounded up
+// to 32, where sample i keeps its row of 32 but its column is rotated by
+// 7 x row, so the two copies of a sample usually sit in different banks.
+// The sort then stores in each resident order slot not the sample index but
+// the shared-memory word to read (copy 0: the index itself; copy 1: base +
+// copy1_offset), choosing the copy so that the 32 positions one sweep gather
+// instruction reads spread over the banks (greedy two-choice assignment:
+// about 2.25 wavefronts per gather instead of 3.5 for one copy).  The sums
+// are unchanged: every position still adds its own sample's weight.
+constexpr int kTwoCopyMax = 24576;
+__host__ __device__ __forceinline__ int two_copy_base(int n) { return (n + 31) & ~31; }
+__host__ __device__ __forceinline__ uint32_t copy1_offset(uint32_t i) {
+    return (i & ~31u) | ((i + 7u * (i >> 5)) & 31u);
+}
+__host__ __device__ __forceinline__ uint32_t copy1_sample(uint32_t r) {
+    return (r & ~31u) | ((r - 7u * (r >> 5)) & 31u);
+}
+// Sample index of a resident order slot value.
+__host__ __device__ __forceinline__ uint32_t slot_sample(uint32_t v, int slotBase) {
+    return (slotBase > 0 && v >= static_cast<uint32_t>(slotBase)) ? copy1_sample(v - slotBase) : v;
+}
+// Fills a block's shared weights: one copy, or both copies when slotBase > 0.
+__device__ __forceinline__ void fill_weights(float* dst, const float* __restrict__ src, int n, int slotBase) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float w = src[i];
+        dst[i] = w;
+        if (slotBase > 0) dst[slotBase + copy1_offset(i)] = w;
+    }
+}
+
 struct RoundParams {
     float tp, tn, w;             // active positive / negative weight and their sum
     float window;                // candidate window above the fast minimum
@@ -104,7 +137,7 @@ __global__ void __launch_bounds__(kSortThreads, 1)
 eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int featCount,
                  const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm, int n,
                  const float* __restrict__ resp, uint16_t* __restrict__ ordOut, int64_t ordStride,
-                 bool ordPadded, uint32_t* __restrict__ gapOut, int64_t gapStride) {
+                 bool ordPadded, uint32_t* __restrict__ gapOut, int64_t gapStride, int slotBase) {
     constexpr int NP = 1024 * R;
     constexpr bool kPP = sort_ping_pong<R>();
     extern __shared__ __align__(16) unsigned char smem[];
@@ -245,15 +278,6 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
             __syncthreads();
         }
 
-        // Sorted sample order (padded rows: chunk-interleaved, see ord_slot).
-        uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
-        if (ordPadded) {
-            const int n8 = (n + 7) & ~7;
-            for (int k = tid * 8; k < n8; k += kSortThreads * 8)
-                *reinterpret_cast<uint4*>(orow + ord_slot(k)) = *reinterpret_cast<const uint4*>(idx + k);
-        } else {
-            for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
-        }
         // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
         // A warp takes 32 consecutive positions per step, one per lane; the
         // next value comes from the next lane, and the word from one ballot.
@@ -267,6 +291,41 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                 const uint32_t bits = __ballot_sync(0xffffffffu, k + 1 < n && __fadd_rn(v0, 1e-7f) < v1);
                 if (lane == 0) grow[k0 >> 5] = bits;
             }
+        }
+        // Two weight copies: pick each position's copy.  The sweep's gather
+        // instruction i of chunk c reads positions c*512 + 16m + i, m = 0..31
+        // (lane m); one thread takes that group and assigns its members in
+        // turn to the less loaded of their two banks (greedy two-choice, loads
+        // tracked up to 2 in two bit masks: o1 = banks with load >= 1, o2 = >= 2).
+        if (ordPadded && slotBase > 0) {
+            __syncthreads();
+            const int groups = ((n + 511) >> 9) * 16;
+            for (int g = tid; g < groups; g += kSortThreads) {
+                const int kb = (g >> 4) * 512 + (g & 15);
+                const int members = min(32, (n - kb + 15) >> 4);
+                uint32_t o1 = 0, o2 = 0;
+                for (int m = 0; m < members; ++m) {
+                    const uint32_t id = idx[kb + 16 * m];
+                    const uint32_t off1 = copy1_offset(id);
+                    const int b0 = id & 31, b1 = off1 & 31;
+                    // copy 1 is less loaded: b0 at 1 and b1 empty, or b0 at 2 and b1 below 2
+                    const bool one = ((o1 >> b0) & 1u) && !((((o2 >> b0) & 1u) ? o2 : o1) >> b1 & 1u);
+                    const uint32_t bit = 1u << (one ? b1 : b0);
+                    o2 |= o1 & bit;
+                    o1 |= bit;
+                    if (one) idx[kb + 16 * m] = static_cast<uint16_t>(slotBase + off1);
+                }
+            }
+            __syncthreads();
+        }
+        // Sorted sample order (padded rows: chunk-interleaved, see ord_slot).
+        uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
+        if (ordPadded) {
+            const int n8 = (n + 7) & ~7;
+            for (int k = tid * 8; k < n8; k += kSortThreads * 8)
+                *reinterpret_cast<uint4*>(orow + ord_slot(k)) = *reinterpret_cast<const uint4*>(idx + k);
+        } else {
+            for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
         }
         __syncthreads();
     }
@@ -347,17 +406,18 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
 // 2. Fast sweep: one warp per feature, minimum weighted error to within the
 //    bound used for the window.
 // ---------------------------------------------------------------------------
-template <bool kSmemW>
-__global__ void __launch_bounds__(kSweepThreads, 2)
+template <bool kSmemW, int TPB>
+__global__ void __launch_bounds__(TPB, 1024 / TPB)
 sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
-             int64_t gapStride, const float* __restrict__ wsgG, int n, int featCount,
+             int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, int featCount,
              const uint8_t* __restrict__ usedMask, RoundParams* __restrict__ prm,
              float* __restrict__ fastErr, const int* gate) {
+    constexpr int kSweepWarps = TPB / 32;
     if (gate_closed(gate)) return;
     extern __shared__ float wsgS[];
     const float* wsg = wsgG;
     if (kSmemW) {
-        for (int i = threadIdx.x; i < n; i += kSweepThreads) wsgS[i] = wsgG[i];
+        fill_weights(wsgS, wsgG, n, slotBase);
         __syncthreads();
         wsg = wsgS;
     }
@@ -512,7 +572,7 @@ __global__ void select_candidates_kernel(const float* __restrict__ fastErr, int 
 template <bool kSmemW>
 __global__ void __launch_bounds__(kRefineThreads)
 refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
-              int64_t gapStride, const float* __restrict__ wsgG, int n, RoundParams* __restrict__ prm,
+              int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, RoundParams* __restrict__ prm,
               const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit,
               unsigned long long* __restrict__ candKey, float2* __restrict__ prefix, int64_t prefixStride,
               const int* gate) {
@@ -522,7 +582,7 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
     __shared__ __align__(16) float2 pre[kRefineWarps][256];    // (left positive, left negative) after each position
     const float* wsg = wsgG;
     if (kSmemW) {
-        for (int i = threadIdx.x; i < n; i += blockDim.x) wsgS[i] = wsgG[i];
+        fill_weights(wsgS, wsgG, n, slotBase);
         __syncthreads();
         wsg = wsgS;
     }
@@ -638,7 +698,7 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
 // 5. Winner -> TileBestCandidate with theta = 0.5f * (v[k] + v[k+1]).
 __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const uint32_t* __restrict__ sumT,
                                 const float* __restrict__ invNorm, int n, const uint16_t* __restrict__ ord,
-                                int64_t ordStride, RoundParams* __restrict__ prm,
+                                int64_t ordStride, int slotBase, RoundParams* __restrict__ prm,
                                 const int8_t* __restrict__ refParity, const int* __restrict__ refSplit,
                                 vj_tile_best* __restrict__ out, const int* gate) {
     if (gate_closed(gate)) return;
@@ -656,7 +716,7 @@ __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const
         const int f = static_cast<int>(w & 0xFFFFFFFFull);
         const int k = refSplit[f];
         const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
-        const int s0 = row[ord_slot(k)], s1 = row[ord_slot(k + 1)];
+        const int s0 = slot_sample(row[ord_slot(k)], slotBase), s1 = slot_sample(row[ord_slot(k + 1)], slotBase);
         const vj_haar_feature ft = feats[f];
         const float v0 = train_response(ft, sumT, n, s0, invNorm[s0]);
         const float v1 = train_response(ft, sumT, n, s1, invNorm[s1]);
@@ -1046,14 +1106,14 @@ int refine_blocks() { return sm_count(); }
 // Launches eval_sort_kernel with the smallest items-per-thread that holds n.
 int launch_eval_sort(const vj_haar_feature* feats, int featBegin, int featCount, const uint32_t* sumT,
                      const float* invNorm, int n, const float* resp, uint16_t* ordOut, int64_t ordStride,
-                     bool ordPadded, uint32_t* gapOut, int64_t gapStride, cudaStream_t stream) {
+                     bool ordPadded, uint32_t* gapOut, int64_t gapStride, int slotBase, cudaStream_t stream) {
     const int grid = std::min(featCount, sm_count());
     auto go = [&](auto kernel, size_t smem) -> int {
         VJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
         VJ_TIMED_LAUNCH("eval_sort_kernel", stream,
                         kernel<<<grid, kSortThreads, smem, stream>>>(feats, featBegin, featCount, sumT, invNorm, n,
                                                                      resp, ordOut, ordStride, ordPadded, gapOut,
-                                                                     gapStride));
+                                                                     gapStride, slotBase));
         VJ_LAUNCH_CHECK("eval_sort_kernel");
         return VJ_OK;
     };
@@ -1091,6 +1151,7 @@ struct vj_trainer {
     uint32_t* d_gap = nullptr;
     size_t ordBytes = 0, gapBytes = 0;
     int64_t ordStride = 0, gapStride = 0;
+    int slotBase = 0;  // > 0: resident orders hold two-copy shared-memory slots
     bool prepared = false;
     // Per-round scratch.
     float* d_wsg = nullptr;
@@ -1179,8 +1240,9 @@ int sort_all(vj_trainer* t, cudaStream_t s) {
     }
     t->ordStride = ordStride;
     t->gapStride = gapStride;
+    t->slotBase = t->n <= kTwoCopyMax ? two_copy_base(t->n) : 0;
     return launch_eval_sort(t->d_feat, 0, static_cast<int>(t->nFeat), t->d_sumT, t->d_invNorm, t->n, nullptr,
-                            t->d_ord, ordStride, true, t->d_gap, gapStride, s);
+                            t->d_ord, ordStride, true, t->d_gap, gapStride, t->slotBase, s);
 }
 
 }  // namespace
@@ -1305,7 +1367,7 @@ int vj_trainer_last_round(vj_trainer* t, vj_round_info* out) {
 
 int vj_trainer_stage_bytes(vj_trainer* t, int n, int64_t* bytes) {
     if (!t || !bytes || n <= 0) return set_error(VJ_INVALID_ARG, "vj_trainer_stage_bytes: bad arguments");
-    *bytes = t->nFeat * (((n + 7) & ~7) * 2 + ((n + 31) / 32) * 4);
+    *bytes = t->nFeat * (((static_cast<int64_t>(n) + 511) & ~int64_t(511)) * 2 + ((n + 31) / 32) * 4);
     return ok();
 }
 
@@ -1341,15 +1403,19 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
                                                          t->d_gate));
     VJ_LAUNCH_CHECK("prep_round_kernel");
     const bool smemW = n <= kSmemWeightsMax;
-    const size_t wbytes = smemW ? sizeof(float) * n : 0;
+    const int sb = t->slotBase;
+    // one copy of the weights per 512-thread block (two blocks per SM), or
+    // both copies in one 1024-thread block per SM
+    const size_t wbytes = !smemW ? 0 : sizeof(float) * (sb > 0 ? 2 * static_cast<size_t>(sb) : n);
     {
-        const int grid = std::min(div_up(F, kSweepWarps), 2 * sm_count());
-        auto k = smemW ? sweep_kernel<true> : sweep_kernel<false>;
+        const int tpb = sb > 0 ? 1024 : kSweepThreads;
+        const int grid = std::min(div_up(F, tpb / 32), (1024 / tpb) * sm_count());
+        auto k = sb > 0 ? sweep_kernel<true, 1024>
+                        : (smemW ? sweep_kernel<true, kSweepThreads> : sweep_kernel<false, kSweepThreads>);
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("sweep_kernel", s,
-                        k<<<grid, kSweepThreads, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride,
-                                                             t->d_wsg, n, F, d_usedMask, t->d_prm, t->d_fastErr,
-                                                             t->d_gate));
+                        k<<<grid, tpb, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb,
+                                                    F, d_usedMask, t->d_prm, t->d_fastErr, t->d_gate));
         VJ_LAUNCH_CHECK("sweep_kernel");
     }
     VJ_TIMED_LAUNCH("select_candidates_kernel", s,
@@ -1361,14 +1427,14 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("refine_kernel", s,
                         k<<<refine_blocks(), kRefineThreads, wbytes, s>>>(
-                            t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, t->d_prm, t->d_cand,
+                            t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb, t->d_prm, t->d_cand,
                             t->d_refParity, t->d_refSplit, t->d_candKey, t->d_prefix, static_cast<int64_t>(t->maxSamples),
                             t->d_gate));
         VJ_LAUNCH_CHECK("refine_kernel");
     }
     VJ_TIMED_LAUNCH("finalize_kernel", s,
                     finalize_kernel<<<1, 32, 0, s>>>(t->d_feat, t->d_sumT, t->d_invNorm, n, t->d_ord, t->ordStride,
-                                                     t->d_prm, t->d_refParity, t->d_refSplit, d_out, t->d_gate));
+                                                     sb, t->d_prm, t->d_refParity, t->d_refSplit, d_out, t->d_gate));
     VJ_LAUNCH_CHECK("finalize_kernel");
     return ok();
 }
@@ -1427,7 +1493,7 @@ int vj_trainer_sort_per_feature(vj_trainer* t, const float* d_resp, int featureC
     if (!t || !d_resp || !d_sortedIdx || featureCount <= 0 || t->n <= 0)
         return set_error(VJ_INVALID_ARG, "vj_trainer_sort_per_feature: bad arguments");
     const int st = launch_eval_sort(nullptr, 0, featureCount, nullptr, nullptr, t->n, d_resp, d_sortedIdx, t->n,
-                                    false, nullptr, 0, static_cast<cudaStream_t>(stream));
+                                    false, nullptr, 0, 0, static_cast<cudaStream_t>(stream));
     return st == VJ_OK ? ok() : st;
 }
 

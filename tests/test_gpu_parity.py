@@ -122,6 +122,30 @@ def test_weak_search_resident_equals_fused(cuda, vj, oracle, gin, basic_pool):
     assert T.search() == fused
 
 
+@pytest.mark.parametrize("n", [24576, 25600])
+def test_weak_search_both_weight_layouts(cuda, vj, oracle, basic_pool, n):
+    """Up to 24,576 samples the resident orders carry slots of two bank-spread
+    weight copies; above that one copy and plain sample indices.  Both give the
+    oracle's pick, round after round."""
+    p = vj.synth_patches(31, n // 2, n // 2)
+    labels = np.array([1] * (n // 2) + [-1] * (n // 2), np.int8)
+    feats = np.ascontiguousarray(basic_pool[::317][:512])
+    rng = np.random.default_rng(n)
+    w = (rng.random(n) / n).astype(np.float32)
+    T = Train(cuda, vj, oracle, p, labels, feats, w)
+    assert T.t.prepareStage() == 0
+    sums, inv = oracle.train_integrals(p)
+    used = np.zeros(len(feats), np.uint8)
+    strong = np.zeros(n, np.float32)
+    weak = cuda.zeros(7, dtype=cuda.int32, device="cuda")
+    for _ in range(3):
+        got = T.search(used=True)
+        ref = oracle.weak_search(feats, sums, inv, labels, T.w.cpu().numpy(), used=used, threads=16)
+        assert got == (ref["featureIdx"], ref["err"], ref["theta"], ref["parity"])
+        assert T.t.applyBestWeak(T.best, T.strong, T.used, weak) == 0
+        used[got[0]] = 1
+
+
 def test_rounds_match_reference_and_oracle(cuda, vj, oracle, golden, basic_pool):
     g = golden["rounds"]
     p = vj.synth_patches(g["seed"], g["npos"], g["nneg"])
