@@ -578,8 +578,9 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
               const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ float wsgS[];
-    __shared__ __align__(16) float stage[kRefineWarps][256];   // gathered weights of one chunk, in order
-    __shared__ __align__(16) float2 pre[kRefineWarps][256];    // (left positive, left negative) after each position
+    // per warp and chunk position: first the (positive, negative) addends of
+    // the position's sample, then, in place, the left sums after it
+    __shared__ __align__(16) float2 pre[kRefineWarps][256];
     const float* wsg = wsgG;
     if (kSmemW) {
         fill_weights(wsgS, wsgG, n, slotBase);
@@ -591,7 +592,8 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
     const int nc = prm->ncand;
     // One warp per candidate feature.  The warp streams the feature's sorted
     // order 256 positions at a time (one coalesced 16-byte load per lane,
-    // issued a chunk ahead), gathers the signed weights into `stage` in
+    // issued a chunk ahead), gathers the signed weights and stores each
+    // position's two addends (|w| to its class's sum, +0.0f to the other) in
     // order, and lane 0 replays the reference's sequential FP32 additions
     // (main.cu:626-678) from there.  Inactive samples carry a zero weight and
     // the accumulator of the other class adds +0.0f: both leave an FP32 sum
@@ -607,16 +609,21 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
         auto gather = [&](int base, const uint4& v) {
             const int k0 = base + lane * 8;
             const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-            float x[8];
+            float4* st = reinterpret_cast<float4*>(&pre[w][lane * 8]);
 #pragma unroll
-            for (int h = 0; h < 8; ++h) {
-                const bool in = k0 + h < n;
-                const uint32_t id = in ? ((w4[h >> 1] >> (16 * (h & 1))) & 0xFFFFu) : 0u;
-                x[h] = in ? wsg[id] : 0.0f;
+            for (int h = 0; h < 8; h += 2) {
+                float ap[2], an[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const bool in = k0 + h + u < n;
+                    const uint32_t id = in ? ((w4[(h + u) >> 1] >> (16 * ((h + u) & 1))) & 0xFFFFu) : 0u;
+                    const float e = in ? wsg[id] : 0.0f;
+                    const bool neg = signbit(e);
+                    ap[u] = neg ? 0.0f : fabsf(e);
+                    an[u] = neg ? fabsf(e) : 0.0f;
+                }
+                st[h >> 1] = make_float4(ap[0], an[0], ap[1], an[1]);
             }
-            float4* st = reinterpret_cast<float4*>(&stage[w][lane * 8]);
-            st[0] = make_float4(x[0], x[1], x[2], x[3]);
-            st[1] = make_float4(x[4], x[5], x[6], x[7]);
         };
         // One sequential pass (lane 0): the left sums after every position, in
         // sorted order, into the warp's row of `prefix`.  Carried on to the last
@@ -631,19 +638,14 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
                 gather(base, v);
                 __syncwarp();
                 if (lane == 0) {
-                    const float4* st = reinterpret_cast<const float4*>(stage[w]);
-#pragma unroll 4
-                    for (int j = 0; j < 64; ++j) {
+                    float4* st = reinterpret_cast<float4*>(pre[w]);
+#pragma unroll 8
+                    for (int j = 0; j < 128; ++j) {
                         const float4 q = st[j];
-                        const float e[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                        for (int h = 0; h < 4; ++h) {
-                            const bool neg = signbit(e[h]);
-                            const float a = fabsf(e[h]);
-                            tp = __fadd_rn(tp, neg ? 0.0f : a);
-                            tn = __fadd_rn(tn, neg ? a : 0.0f);
-                            pre[w][4 * j + h] = make_float2(tp, tn);
-                        }
+                        const float p0 = __fadd_rn(tp, q.x), n0 = __fadd_rn(tn, q.y);
+                        tp = __fadd_rn(p0, q.z);
+                        tn = __fadd_rn(n0, q.w);
+                        st[j] = make_float4(p0, n0, tp, tn);
                     }
                 }
                 __syncwarp();
