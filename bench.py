@@ -311,10 +311,10 @@ def run_gpu(args, rank, world):
     }.get(name)
     avg_ms = total / max(1, launches)
     # DRAM bytes (read + write) per feature-sample of one launch, from ncu's
-    # dram__bytes counters on the 16,384-feature x 20,000-sample case
-    # (profiles/stump_kernels_16k_features.md), scaled to this launch's size.
-    traffic_per_unit = {"sweep_kernel": (699.499008e6 + 3.169280e6) / (16384 * 20000),
-                        "eval_sort_kernel": (351.887872e6 + 729.445632e6) / (16384 * 20000)}.get(name)
+    # dram__bytes counters on the 16,384-feature x 20,000-sample case, scaled
+    # to this launch's size.
+    traffic_per_unit = {"sweep_kernel": (701.433600e6 + 3.959296e6) / (16384 * 20000),
+                        "eval_sort_kernel": (235.247616e6 + 659.254784e6) / (16384 * 20000)}.get(name)
     roof = {"kernel": name, "bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
             "avg_launch_ms": avg_ms, "launches": launches, "share_of_step": total / ms if ms else None,
             "traffic": traffic_per_unit * F * n if traffic_per_unit else None,
