@@ -209,12 +209,14 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
 #pragma unroll
             for (int j = 0; j < R; ++j) {
                 const uint32_t d = (dig[j >> 2] >> (8 * (j & 3))) & 255u;
-                uint32_t peers = 0xffffffffu;
+                // lanes whose digit differs in some bit: ballot XOR the lane's own bit, sign-extended
+                uint32_t differ = 0;
 #pragma unroll
                 for (int b = 0; b < 8; ++b) {
                     const uint32_t m = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-                    peers &= ((d >> b) & 1u) ? m : ~m;
+                    differ |= m ^ (0u - ((d >> b) & 1u));
                 }
+                const uint32_t peers = ~differ;
                 const int leader = __ffs(peers) - 1;
                 uint32_t old = 0;
                 if (lane == leader) {
