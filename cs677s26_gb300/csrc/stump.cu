@@ -208,7 +208,7 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
             }
 #pragma unroll
             for (int j = 0; j < R; ++j) {
-                const uint32_t d = (dig[j >> 2] >> (8 * (j & 3))) & 255u;
+                const uint32_t d = __byte_perm(dig[j >> 2], 0u, 0x4440u | static_cast<uint32_t>(j & 3));
                 // lanes whose digit differs in some bit: ballot XOR the lane's own bit, sign-extended
                 uint32_t differ = 0;
 #pragma unroll
@@ -217,14 +217,14 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                     differ |= m ^ (0u - ((d >> b) & 1u));
                 }
                 const uint32_t peers = ~differ;
-                const int leader = __ffs(peers) - 1;
-                uint32_t old = 0;
-                if (lane == leader) {
-                    old = cnt[d * kCntStride + warp];
-                    cnt[d * kCntStride + warp] = old + __popc(peers);
-                }
-                old = __shfl_sync(0xffffffffu, old, leader);
-                const uint32_t rank = old + __popc(peers & lanemask_lt());
+                // every lane reads its digit's counter; once the warp has read,
+                // the first lane of each equal-digit group stores the new count
+                const uint32_t before = peers & lanemask_lt();
+                const uint32_t old = cnt[d * kCntStride + warp];
+                __syncwarp();
+                if (before == 0) cnt[d * kCntStride + warp] = old + __popc(peers);
+                __syncwarp();
+                const uint32_t rank = old + __popc(before);
                 if (kPP)
                     packed[j >> 1] |= rank << (16 * (j & 1));
                 else
@@ -268,7 +268,7 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
             __syncthreads();
 #pragma unroll
             for (int j = 0; j < R; ++j) {
-                const uint32_t d = (dig[j >> 2] >> (8 * (j & 3))) & 255u;
+                const uint32_t d = __byte_perm(dig[j >> 2], 0u, 0x4440u | static_cast<uint32_t>(j & 3));
                 if (kPP) {
                     const uint32_t rank = (packed[j >> 1] >> (16 * (j & 1))) & 0xFFFFu;
                     dst[cnt[d * kCntStride + warp] + rank] = src[warp * 32 * R + j * 32 + lane];
