@@ -146,6 +146,51 @@ def test_weak_search_both_weight_layouts(cuda, vj, oracle, basic_pool, n):
         used[got[0]] = 1
 
 
+@pytest.mark.parametrize("n", [2, 3, 17, 33, 100, 511, 513, 1000])
+def test_weak_search_small_and_ragged_counts(cuda, vj, oracle, basic_pool, n):
+    """Sample counts around the sweep's 16-position lane runs, its 512-position
+    chunks and the 32-member copy-assignment groups: the oracle's pick, two
+    rounds in a row, with the resident orders."""
+    npos = max(1, n // 2)
+    p = vj.synth_patches(40 + n, npos, n - npos)
+    labels = np.array([1] * npos + [-1] * (n - npos), np.int8)
+    feats = np.ascontiguousarray(basic_pool[::53][:3000])
+    rng = np.random.default_rng(n)
+    w = (rng.random(n) / n).astype(np.float32)
+    T = Train(cuda, vj, oracle, p, labels, feats, w)
+    assert T.t.prepareStage() == 0
+    sums, inv = oracle.train_integrals(p)
+    used = np.zeros(len(feats), np.uint8)
+    weak = cuda.zeros(7, dtype=cuda.int32, device="cuda")
+    for _ in range(2):
+        got = T.search(used=True)
+        ref = oracle.weak_search(feats, sums, inv, labels, T.w.cpu().numpy(), used=used, threads=8)
+        assert got == (ref["featureIdx"], ref["err"], ref["theta"], ref["parity"])
+        if got[0] < 0:
+            break
+        assert T.t.applyBestWeak(T.best, T.strong, T.used, weak) == 0
+        used[got[0]] = 1
+
+
+def test_weak_search_without_valid_split(cuda, vj, oracle, basic_pool):
+    """Identical patches give every feature a single value: no valid split
+    anywhere, reported as featureIdx -1 with an infinite error, as the oracle
+    does."""
+    one = vj.synth_patches(5, 1, 0)
+    p = np.ascontiguousarray(np.repeat(one, 40, axis=0))
+    labels = np.array([1] * 20 + [-1] * 20, np.int8)
+    feats = np.ascontiguousarray(basic_pool[:2000])
+    w = np.full(40, np.float32(1.0 / 40), np.float32)
+    T = Train(cuda, vj, oracle, p, labels, feats, w)
+    sums, inv = oracle.train_integrals(p)
+    ref = oracle.weak_search(feats, sums, inv, labels, w)
+    assert ref["featureIdx"] == -1
+    got = T.search()
+    assert got[0] == -1 and got[1] == float("inf") and got[3] == ref["parity"]
+    assert T.t.prepareStage() == 0
+    assert T.search() == got
+
+
 def test_rounds_match_reference_and_oracle(cuda, vj, oracle, golden, basic_pool):
     g = golden["rounds"]
     p = vj.synth_patches(g["seed"], g["npos"], g["nneg"])
