@@ -18,8 +18,9 @@
 //      conflicts in the sweep) and a bitmask of valid split positions
 //      (v[k] + 1e-7f < v[k+1], boosting_core.cu:400).
 //   2. sweep_kernel: one warp per feature streams that order, gathers signed
-//      weights from shared memory and forms FP32 prefix sums (8-element lane
-//      runs, warp shuffle scan, Kahan-compensated carries across chunks) to
+//      weights from shared memory and forms FP32 prefix sums (each lane a run
+//      of the feature's sorted positions, 16 at a time with a Kahan-compensated
+//      carry, one warp shuffle scan per feature) to
 //      get each feature's minimum weighted error to within a proven bound.
 //   3. Candidates: every feature whose error is within 2*(bound of the
 //      reference's sequential FP32 arithmetic + bound of step 2) of the
@@ -63,17 +64,25 @@ __device__ __forceinline__ bool gate_closed(const int* g) {
     return g != nullptr && *reinterpret_cast<const volatile int*>(g) != 0;
 }
 
-// Resident stage orders (one row per feature) are stored chunk-interleaved:
-// in each chunk of 512 sorted positions, positions 16l..16l+7 sit at slots
-// 8l..8l+7 and positions 16l+8..16l+15 at slots 256+8l..256+8l+7.  A sweep
-// lane owns the 16 consecutive positions 16l..16l+15 of a chunk, and with
-// this layout each of its two 16-byte loads is contiguous across the warp
-// (512 B per load instruction instead of 1 KB half-used).  Any 8 consecutive
-// positions starting at a multiple of 8 stay contiguous.  Rows are padded to
-// a multiple of 512 positions.
-__host__ __device__ __forceinline__ int64_t ord_slot(int64_t k) {
-    const int64_t r = k & 511;
-    return (k - r) + ((r >> 3) & 1) * 256 + (r >> 4) * 8 + (r & 7);
+// Resident stage orders (one row per feature) are stored by lane runs: the
+// sweep's lane l owns the L consecutive sorted positions [l*L, (l+1)*L), with
+// L = lane_run(n) = ceil(n / 32) rounded up to 16, and step t of a row (256
+// slots) holds positions l*L + 8t .. l*L + 8t + 7 of every lane l at slots
+// 256t + 8l .. 256t + 8l + 7.  Each 16-byte load of a lane is thus contiguous
+// across the warp (512 B per load instruction), and any 8 positions starting
+// at a multiple of 8 stay contiguous.  Rows are 32*L positions; positions from
+// n up to the next multiple of 8 hold the zero-weight slot (zero_slot).  The
+// split bitmask is stored the same way: 16-bit word 32*t + l holds the bits of
+// positions l*L + 16t .. l*L + 16t + 15.
+__host__ __device__ __forceinline__ int lane_run(int n) { return (((n + 31) / 32) + 15) & ~15; }
+// (positions and slots are below 32 * 1024, so 32-bit arithmetic is exact)
+__host__ __device__ __forceinline__ int ord_slot(int k, int L) {
+    const int l = k / L, r = k - l * L;
+    return (r >> 3) * 256 + l * 8 + (r & 7);
+}
+__host__ __device__ __forceinline__ int gap_word(int k, int L) {
+    const int l = k / L, r = k - l * L;
+    return (r >> 4) * 32 + l;
 }
 
 // Two copies of the round's signed weights in shared memory (n <= kTwoCopyMax):
@@ -94,17 +103,22 @@ __host__ __device__ __forceinline__ uint32_t copy1_offset(uint32_t i) {
 __host__ __device__ __forceinline__ uint32_t copy1_sample(uint32_t r) {
     return (r & ~31u) | ((r - 7u * (r >> 5)) & 31u);
 }
+// Shared-memory word that holds +0.0f, after the weights: the slot of the
+// padding positions, so a lane past n adds nothing and needs no mask.
+__host__ __device__ __forceinline__ int zero_slot(int n, int slotBase) { return slotBase > 0 ? 2 * slotBase : n; }
 // Sample index of a resident order slot value.
 __host__ __device__ __forceinline__ uint32_t slot_sample(uint32_t v, int slotBase) {
     return (slotBase > 0 && v >= static_cast<uint32_t>(slotBase)) ? copy1_sample(v - slotBase) : v;
 }
-// Fills a block's shared weights: one copy, or both copies when slotBase > 0.
+// Fills a block's shared weights: one copy, or both copies when slotBase > 0,
+// and the zero slot.
 __device__ __forceinline__ void fill_weights(float* dst, const float* __restrict__ src, int n, int slotBase) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float w = src[i];
         dst[i] = w;
         if (slotBase > 0) dst[slotBase + copy1_offset(i)] = w;
     }
+    if (threadIdx.x == 0) dst[zero_slot(n, slotBase)] = 0.0f;
 }
 
 struct RoundParams {
@@ -137,7 +151,7 @@ __global__ void __launch_bounds__(kSortThreads, 1)
 eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int featCount,
                  const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm, int n,
                  const float* __restrict__ resp, uint16_t* __restrict__ ordOut, int64_t ordStride,
-                 bool ordPadded, uint32_t* __restrict__ gapOut, int64_t gapStride, int slotBase) {
+                 bool ordPadded, uint16_t* __restrict__ gapOut, int64_t gapStride, int slotBase, int L) {
     constexpr int NP = 1024 * R;
     constexpr bool kPP = sort_ping_pong<R>();
     extern __shared__ __align__(16) unsigned char smem[];
@@ -283,31 +297,37 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
         // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
         // A warp takes 32 consecutive positions per step, one per lane; the
         // next value comes from the next lane, and the word from one ballot.
+        // The words (in the free digit-counter array) are then stored in the
+        // lane-run layout of the resident orders (see ord_slot).
         if (gapOut) {
-            uint32_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
+            uint32_t* gnat = cnt;
             for (int k0 = warp * 32; k0 < gapWords * 32; k0 += kSortThreads) {
                 const int k = k0 + lane;
                 const float v0 = k < n ? __uint_as_float(radix_key_inv(keys[idx[k]])) : 0.0f;
                 float v1 = __shfl_down_sync(0xffffffffu, v0, 1);
                 if (lane == 31 && k + 1 < n) v1 = __uint_as_float(radix_key_inv(keys[idx[k + 1]]));
                 const uint32_t bits = __ballot_sync(0xffffffffu, k + 1 < n && __fadd_rn(v0, 1e-7f) < v1);
-                if (lane == 0) grow[k0 >> 5] = bits;
+                if (lane == 0) gnat[k0 >> 5] = bits;
+            }
+            __syncthreads();
+            uint16_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
+            for (int j = tid; j < 2 * L; j += kSortThreads) {
+                const int k = (j & 31) * L + 16 * (j >> 5);  // first position of the word
+                grow[j] = k < n ? static_cast<uint16_t>(gnat[k >> 5] >> (k & 31)) : uint16_t(0);
             }
         }
         // Two weight copies: pick each position's copy.  The sweep's gather
-        // instruction i of chunk c reads positions c*512 + 16m + i, m = 0..31
+        // instruction i of step t reads positions m*L + 16t + i, m = 0..31
         // (lane m); one thread takes that group and assigns its members in
         // turn to the less loaded of their two banks (greedy two-choice, loads
         // tracked up to 2 in two bit masks: o1 = banks with load >= 1, o2 = >= 2).
         if (ordPadded && slotBase > 0) {
             __syncthreads();
-            const int groups = ((n + 511) >> 9) * 16;
-            for (int g = tid; g < groups; g += kSortThreads) {
-                const int kb = (g >> 4) * 512 + (g & 15);
-                const int members = min(32, (n - kb + 15) >> 4);
+            for (int g = tid; g < L; g += kSortThreads) {
+                const int kb = 16 * (g >> 4) + (g & 15);
                 uint32_t o1 = 0, o2 = 0;
-                for (int m = 0; m < members; ++m) {
-                    const uint32_t id = idx[kb + 16 * m];
+                for (int m = 0; m < 32 && kb + m * L < n; ++m) {
+                    const uint32_t id = idx[kb + m * L];
                     const uint32_t off1 = copy1_offset(id);
                     const int b0 = id & 31, b1 = off1 & 31;
                     // copy 1 is less loaded: b0 at 1 and b1 empty, or b0 at 2 and b1 below 2
@@ -315,17 +335,19 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                     const uint32_t bit = 1u << (one ? b1 : b0);
                     o2 |= o1 & bit;
                     o1 |= bit;
-                    if (one) idx[kb + 16 * m] = static_cast<uint16_t>(slotBase + off1);
+                    if (one) idx[kb + m * L] = static_cast<uint16_t>(slotBase + off1);
                 }
             }
             __syncthreads();
         }
-        // Sorted sample order (padded rows: chunk-interleaved, see ord_slot).
+        // Sorted sample order (padded rows: lane runs, see ord_slot).
         uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
         if (ordPadded) {
             const int n8 = (n + 7) & ~7;
+            if (tid < n8 - n) idx[n + tid] = static_cast<uint16_t>(zero_slot(n, slotBase));
+            __syncthreads();
             for (int k = tid * 8; k < n8; k += kSortThreads * 8)
-                *reinterpret_cast<uint4*>(orow + ord_slot(k)) = *reinterpret_cast<const uint4*>(idx + k);
+                *reinterpret_cast<uint4*>(orow + ord_slot(k, L)) = *reinterpret_cast<const uint4*>(idx + k);
         } else {
             for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
         }
@@ -346,6 +368,7 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
     __shared__ int cp[32], cn[32];
     double tp = 0.0, tn = 0.0;
     int np = 0, nn = 0;
+    if (threadIdx.x == 0) wsg[n] = 0.0f;  // the zero slot of one-copy orders
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const bool act = active == nullptr || active[i] != 0;
         const float w = act ? weight[i] : 0.0f;
@@ -389,6 +412,11 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
         const double W = TP + TN;
         // |sequential FP32 error - exact| for either parity (see the header).
         const double bcpu = 2.0 * gamma(NP + 2) * TP + 2.0 * gamma(NN + 2) * TN + 4.0 * u * W;
+        // fast pass: a position's prefix is fl(E + fl(b + s)) with s a sum of
+        // <= 16 terms (15 roundings), b the lane's Kahan carry of its earlier
+        // 16-term step sums (15 + 2 roundings over the lane's mass), E the
+        // warp-scanned sum of the earlier lanes' carries (17 + 5 over theirs),
+        // then 1 + 1 additions and the final difference: <= 25 u W, taken as 64.
         const double bfast = 64.0 * u * W;
         const double window = 2.0 * (bcpu + bfast) * 1.01 + 1e-30;
         prm->tp = static_cast<float>(TP);
@@ -410,8 +438,8 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
 // ---------------------------------------------------------------------------
 template <bool kSmemW, int TPB>
 __global__ void __launch_bounds__(TPB, 1024 / TPB)
-sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
-             int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, int featCount,
+sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t* __restrict__ gap,
+             int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, int L, int featCount,
              const uint8_t* __restrict__ usedMask, RoundParams* __restrict__ prm,
              float* __restrict__ fastErr, const int* gate) {
     constexpr int kSweepWarps = TPB / 32;
@@ -427,115 +455,107 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t
     // two parities' errors at split k are T+ - P(k) and T- + P(k), so a
     // feature's best error is min(T+ - max P, T- + min P) over valid splits.
     //
-    // Each warp walks the flattened sequence of (feature, chunk) items of the
-    // features it owns; a chunk is 512 positions, 16 per lane (two 16-byte
-    // index loads + 16 split bits).  The loads of the next item are issued
-    // before the current one is processed, across feature boundaries, so each
-    // warp keeps two chunks of index traffic in flight.
+    // One warp per feature at a time.  Lane l walks its run of L sorted
+    // positions [l*L, (l+1)*L) 16 at a time (two 16-byte slot loads, 16 split
+    // bits) with a lane-local running sum, Kahan-compensated across steps, and
+    // keeps the minimum and maximum of that sum over its valid splits; at the
+    // feature's end one warp scan gives each lane the sum of the runs before
+    // its own, which is added once.  Rounding is monotone, so
+    // min_i fl(b + s_i) = fl(b + min_i s_i).  Padding positions carry the zero
+    // slot and no split bit, so no position needs a mask.  Each warp walks the
+    // flattened sequence of (feature, step) items of the features it owns; the
+    // loads of the next item are issued before the current one is processed,
+    // across feature boundaries.
     const float TP = prm->tp, TN = prm->tn;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
     const int nw = gridDim.x * kSweepWarps;
-    const int cpf = (n - 1 + 511) / 512;                     // chunks per feature (split positions 0..n-2)
+    const int spf = L >> 4;  // steps per feature
     const int myFeat = gw < featCount ? (featCount - gw + nw - 1) / nw : 0;
-    const int items = myFeat * cpf;
-    // (f, c): feature and chunk of the item to load next.  Used features are
-    // streamed like the others and dropped at the end, so no load waits on
-    // the mask.
-    auto load = [&](int it, int f, int c, uint4& a, uint4& b, uint32_t& g) {
-        a = b = make_uint4(0, 0, 0, 0);
+    const int items = myFeat * spf;
+    const uint32_t z = static_cast<uint32_t>(zero_slot(n, slotBase)) * 0x10001u;
+    // Used features are streamed like the others and dropped at the end, so
+    // no load waits on the mask.
+    auto load = [&](int it, int f, int t, uint4& a, uint4& b, uint32_t& g) {
+        a = b = make_uint4(z, z, z, z);
         g = 0;
         if (it >= items) return;
-        const int k0 = c * 512 + lane * 16;
-        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride + c * 512 + lane * 8;  // ord_slot(k0)
+        const int k0 = lane * L + 16 * t;
+        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride + 512 * t + lane * 8;  // ord_slot(k0, L)
         if (k0 < n) a = __ldg(reinterpret_cast<const uint4*>(row));
         if (k0 + 8 < n) b = __ldg(reinterpret_cast<const uint4*>(row + 256));
-        if (k0 < n - 1) g = (__ldg(gap + static_cast<size_t>(f) * gapStride + (k0 >> 5)) >> (k0 & 31)) & 0xFFFFu;
+        if (k0 < n - 1) g = __ldg(gap + static_cast<size_t>(f) * gapStride + 32 * t + lane);  // gap_word(k0, L)
     };
     float blockMin = INFINITY;
     uint4 ca, cb;
     uint32_t cg;
-    int f = gw, c = 0;        // item being processed
-    int fn = gw, cn = 1;      // item being loaded
-    if (cn == cpf) {
-        cn = 0;
+    int f = gw, t = 0;     // item being processed
+    int fn = gw, tn = 1;   // item being loaded
+    if (tn == spf) {
+        tn = 0;
         fn += nw;
     }
-    load(0, f, c, ca, cb, cg);
+    load(0, f, t, ca, cb, cg);
     float carry = 0.0f, comp = 0.0f, pmin = INFINITY, pmax = -INFINITY;
     for (int it = 0; it < items; ++it) {
         uint4 na, nb;
         uint32_t ng;
-        load(it + 1, fn, cn, na, nb, ng);
-        if (++cn == cpf) {
-            cn = 0;
+        load(it + 1, fn, tn, na, nb, ng);
+        if (++tn == spf) {
+            tn = 0;
             fn += nw;
         }
-        const int k0 = c * 512 + lane * 16;
         const uint32_t w8[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
-        // Lane-local running prefix s; its minimum and maximum over the valid
-        // split positions.  Rounding is monotone, so min_i fl(b + s_i) equals
-        // fl(b + min_i s_i): the chunk base b is added once per lane.
         float s = 0.0f, lmin = INFINITY, lmax = -INFINITY;
-        if (k0 + 16 <= n) {
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                s = __fadd_rn(s, wsg[(w8[i >> 1] >> (16 * (i & 1))) & 0xFFFFu]);
-                if ((cg >> i) & 1u) {
-                    lmin = fminf(lmin, s);
-                    lmax = fmaxf(lmax, s);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                // positions past n hold padding indices: read sample 0, add nothing
-                const bool in = k0 + i < n;
-                const uint32_t id = in ? ((w8[i >> 1] >> (16 * (i & 1))) & 0xFFFFu) : 0u;
-                s = __fadd_rn(s, in ? wsg[id] : 0.0f);
-                if ((cg >> i) & 1u) {
-                    lmin = fminf(lmin, s);
-                    lmax = fmaxf(lmax, s);
-                }
+        for (int i = 0; i < 16; ++i) {
+            s = __fadd_rn(s, wsg[(w8[i >> 1] >> (16 * (i & 1))) & 0xFFFFu]);
+            if ((cg >> i) & 1u) {
+                lmin = fminf(lmin, s);
+                lmax = fmaxf(lmax, s);
             }
         }
-        float incl = s;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const float y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl = __fadd_rn(incl, y);
-        }
-        float excl = __shfl_up_sync(0xffffffffu, incl, 1);
-        if (lane == 0) excl = 0.0f;
-        const float tot = __shfl_sync(0xffffffffu, incl, 31);
-        const float b0 = __fadd_rn(carry, excl);
         if (lmax > -INFINITY) {
-            pmin = fminf(pmin, __fadd_rn(b0, lmin));
-            pmax = fmaxf(pmax, __fadd_rn(b0, lmax));
+            pmin = fminf(pmin, __fadd_rn(carry, lmin));
+            pmax = fmaxf(pmax, __fadd_rn(carry, lmax));
         }
         {
-            const float y = __fsub_rn(tot, comp);
-            const float t = __fadd_rn(carry, y);
-            comp = __fsub_rn(__fsub_rn(t, carry), y);
-            carry = t;
+            const float y = __fsub_rn(s, comp);
+            const float u = __fadd_rn(carry, y);
+            comp = __fsub_rn(__fsub_rn(u, carry), y);
+            carry = u;
         }
-        if (c == cpf - 1) {
+        if (t == spf - 1) {
+            // exclusive prefix of the lanes' run sums
+            float incl = carry;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl = __fadd_rn(incl, y);
+            }
+            float excl = __shfl_up_sync(0xffffffffu, incl, 1);
+            if (lane == 0) excl = 0.0f;
+            float lo = INFINITY, hi = -INFINITY;
+            if (pmax > -INFINITY) {
+                lo = __fadd_rn(excl, pmin);
+                hi = __fadd_rn(excl, pmax);
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                pmin = fminf(pmin, __shfl_xor_sync(0xffffffffu, pmin, o));
-                pmax = fmaxf(pmax, __shfl_xor_sync(0xffffffffu, pmax, o));
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
             }
             float best = INFINITY;
-            if (pmax > -INFINITY && !(usedMask && usedMask[f]))
-                best = fmaxf(fminf(__fsub_rn(TP, pmax), __fadd_rn(TN, pmin)), 0.0f);
+            if (hi > -INFINITY && !(usedMask && usedMask[f]))
+                best = fmaxf(fminf(__fsub_rn(TP, hi), __fadd_rn(TN, lo)), 0.0f);
             if (lane == 0) fastErr[f] = best;
             blockMin = fminf(blockMin, best);
             carry = comp = 0.0f;
             pmin = INFINITY;
             pmax = -INFINITY;
         }
-        if (++c == cpf) {
-            c = 0;
+        if (++t == spf) {
+            t = 0;
             f += nw;
         }
         ca = na;
@@ -573,8 +593,9 @@ __global__ void select_candidates_kernel(const float* __restrict__ fastErr, int 
 // ---------------------------------------------------------------------------
 template <bool kSmemW>
 __global__ void __launch_bounds__(kRefineThreads)
-refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_t* __restrict__ gap,
-              int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, RoundParams* __restrict__ prm,
+refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t* __restrict__ gap,
+              int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, int L,
+              RoundParams* __restrict__ prm,
               const int* __restrict__ cand, int8_t* __restrict__ refParity, int* __restrict__ refSplit,
               unsigned long long* __restrict__ candKey, float2* __restrict__ prefix, int64_t prefixStride,
               const int* gate) {
@@ -603,10 +624,10 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
     for (int c = blockIdx.x * kRefineWarps + w; c < nc; c += gridDim.x * kRefineWarps) {
         const int f = cand[c];
         const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
-        const uint32_t* grow = gap + static_cast<size_t>(f) * gapStride;
+        const uint16_t* grow = gap + static_cast<size_t>(f) * gapStride;
         auto load = [&](int base) {
             const int k0 = base + lane * 8;
-            return (k0 < n) ? __ldg(reinterpret_cast<const uint4*>(row + ord_slot(k0))) : make_uint4(0, 0, 0, 0);
+            return (k0 < n) ? __ldg(reinterpret_cast<const uint4*>(row + ord_slot(k0, L))) : make_uint4(0, 0, 0, 0);
         };
         auto gather = [&](int base, const uint4& v) {
             const int k0 = base + lane * 8;
@@ -670,7 +691,10 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
         unsigned long long best = ~0ull;
         for (int base = 0; base < n - 1; base += 256) {
             const int k0 = base + lane * 8;
-            const uint32_t g = (k0 < n - 1) ? (__ldg(grow + (k0 >> 5)) >> (k0 & 31)) & 0xFFu : 0u;
+            // the 8 split bits of positions k0..k0+7 (one lane run, one bitmask word)
+            const int l = k0 / L, r = k0 - l * L;
+            const uint32_t g =
+                (k0 < n - 1) ? (static_cast<uint32_t>(__ldg(grow + (r >> 4) * 32 + l)) >> (r & 15)) & 0xFFu : 0u;  // gap_word
 #pragma unroll
             for (int h = 0; h < 8; ++h) {
                 if ((g >> h) & 1u) {
@@ -702,7 +726,7 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint32_
 // 5. Winner -> TileBestCandidate with theta = 0.5f * (v[k] + v[k+1]).
 __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const uint32_t* __restrict__ sumT,
                                 const float* __restrict__ invNorm, int n, const uint16_t* __restrict__ ord,
-                                int64_t ordStride, int slotBase, RoundParams* __restrict__ prm,
+                                int64_t ordStride, int slotBase, int L, RoundParams* __restrict__ prm,
                                 const int8_t* __restrict__ refParity, const int* __restrict__ refSplit,
                                 vj_tile_best* __restrict__ out, const int* gate) {
     if (gate_closed(gate)) return;
@@ -720,7 +744,7 @@ __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const
         const int f = static_cast<int>(w & 0xFFFFFFFFull);
         const int k = refSplit[f];
         const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
-        const int s0 = slot_sample(row[ord_slot(k)], slotBase), s1 = slot_sample(row[ord_slot(k + 1)], slotBase);
+        const int s0 = slot_sample(row[ord_slot(k, L)], slotBase), s1 = slot_sample(row[ord_slot(k + 1, L)], slotBase);
         const vj_haar_feature ft = feats[f];
         const float v0 = train_response(ft, sumT, n, s0, invNorm[s0]);
         const float v1 = train_response(ft, sumT, n, s1, invNorm[s1]);
@@ -1110,14 +1134,14 @@ int refine_blocks() { return sm_count(); }
 // Launches eval_sort_kernel with the smallest items-per-thread that holds n.
 int launch_eval_sort(const vj_haar_feature* feats, int featBegin, int featCount, const uint32_t* sumT,
                      const float* invNorm, int n, const float* resp, uint16_t* ordOut, int64_t ordStride,
-                     bool ordPadded, uint32_t* gapOut, int64_t gapStride, int slotBase, cudaStream_t stream) {
+                     bool ordPadded, uint16_t* gapOut, int64_t gapStride, int slotBase, int L, cudaStream_t stream) {
     const int grid = std::min(featCount, sm_count());
     auto go = [&](auto kernel, size_t smem) -> int {
         VJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
         VJ_TIMED_LAUNCH("eval_sort_kernel", stream,
                         kernel<<<grid, kSortThreads, smem, stream>>>(feats, featBegin, featCount, sumT, invNorm, n,
                                                                      resp, ordOut, ordStride, ordPadded, gapOut,
-                                                                     gapStride, slotBase));
+                                                                     gapStride, slotBase, L));
         VJ_LAUNCH_CHECK("eval_sort_kernel");
         return VJ_OK;
     };
@@ -1152,10 +1176,11 @@ struct vj_trainer {
     float* d_weight = nullptr;
     // Per-feature sample orders and valid-split masks.
     uint16_t* d_ord = nullptr;
-    uint32_t* d_gap = nullptr;
+    uint16_t* d_gap = nullptr;
     size_t ordBytes = 0, gapBytes = 0;
     int64_t ordStride = 0, gapStride = 0;
     int slotBase = 0;  // > 0: resident orders hold two-copy shared-memory slots
+    int laneRun = 16;  // L of the resident layout (lane_run(n))
     bool prepared = false;
     // Per-round scratch.
     float* d_wsg = nullptr;
@@ -1199,7 +1224,7 @@ int ensure_round_scratch(vj_trainer* t) {
     t->scratchFeat = t->scratchN = 0;
     const int64_t F = t->nFeat > 0 ? t->nFeat : 1;
     const int N = t->maxSamples;
-    VJ_CUDA_TRY(cudaMalloc(&t->d_wsg, sizeof(float) * N));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_wsg, sizeof(float) * (N + 1)));  // + the zero slot at n
     VJ_CUDA_TRY(cudaMalloc(&t->d_fastErr, sizeof(float) * F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_cand, sizeof(int) * F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_candKey, sizeof(unsigned long long) * F));
@@ -1224,10 +1249,11 @@ int check_bound(vj_trainer* t, const char* fn) {
 
 // Writes the per-feature orders and split masks for the whole pool.
 int sort_all(vj_trainer* t, cudaStream_t s) {
-    const int64_t ordStride = (static_cast<int64_t>(t->n) + 511) & ~int64_t(511);  // whole 512-position chunks
-    const int64_t gapStride = (t->n + 31) / 32;
+    const int L = lane_run(t->n);
+    const int64_t ordStride = 32 * static_cast<int64_t>(L);  // 32 lane runs
+    const int64_t gapStride = 2 * static_cast<int64_t>(L);   // 16-bit words
     const size_t ordBytes = static_cast<size_t>(t->nFeat) * ordStride * sizeof(uint16_t);
-    const size_t gapBytes = static_cast<size_t>(t->nFeat) * gapStride * sizeof(uint32_t);
+    const size_t gapBytes = static_cast<size_t>(t->nFeat) * gapStride * sizeof(uint16_t);
     if (ordBytes > t->ordBytes) {
         cudaFree(t->d_ord);
         t->d_ord = nullptr;
@@ -1245,8 +1271,9 @@ int sort_all(vj_trainer* t, cudaStream_t s) {
     t->ordStride = ordStride;
     t->gapStride = gapStride;
     t->slotBase = t->n <= kTwoCopyMax ? two_copy_base(t->n) : 0;
+    t->laneRun = L;
     return launch_eval_sort(t->d_feat, 0, static_cast<int>(t->nFeat), t->d_sumT, t->d_invNorm, t->n, nullptr,
-                            t->d_ord, ordStride, true, t->d_gap, gapStride, t->slotBase, s);
+                            t->d_ord, ordStride, true, t->d_gap, gapStride, t->slotBase, L, s);
 }
 
 }  // namespace
@@ -1371,7 +1398,7 @@ int vj_trainer_last_round(vj_trainer* t, vj_round_info* out) {
 
 int vj_trainer_stage_bytes(vj_trainer* t, int n, int64_t* bytes) {
     if (!t || !bytes || n <= 0) return set_error(VJ_INVALID_ARG, "vj_trainer_stage_bytes: bad arguments");
-    *bytes = t->nFeat * (((static_cast<int64_t>(n) + 511) & ~int64_t(511)) * 2 + ((n + 31) / 32) * 4);
+    *bytes = t->nFeat * (static_cast<int64_t>(lane_run(n)) * (32 * 2 + 2 * 2));
     return ok();
 }
 
@@ -1410,7 +1437,7 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
     const int sb = t->slotBase;
     // one copy of the weights per 512-thread block (two blocks per SM), or
     // both copies in one 1024-thread block per SM
-    const size_t wbytes = !smemW ? 0 : sizeof(float) * (sb > 0 ? 2 * static_cast<size_t>(sb) : n);
+    const size_t wbytes = !smemW ? 0 : sizeof(float) * (static_cast<size_t>(zero_slot(n, sb)) + 1);
     {
         const int tpb = sb > 0 ? 1024 : kSweepThreads;
         const int grid = std::min(div_up(F, tpb / 32), (1024 / tpb) * sm_count());
@@ -1419,7 +1446,7 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("sweep_kernel", s,
                         k<<<grid, tpb, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb,
-                                                    F, d_usedMask, t->d_prm, t->d_fastErr, t->d_gate));
+                                                    t->laneRun, F, d_usedMask, t->d_prm, t->d_fastErr, t->d_gate));
         VJ_LAUNCH_CHECK("sweep_kernel");
     }
     VJ_TIMED_LAUNCH("select_candidates_kernel", s,
@@ -1431,14 +1458,16 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("refine_kernel", s,
                         k<<<refine_blocks(), kRefineThreads, wbytes, s>>>(
-                            t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb, t->d_prm, t->d_cand,
+                            t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb, t->laneRun, t->d_prm,
+                            t->d_cand,
                             t->d_refParity, t->d_refSplit, t->d_candKey, t->d_prefix, static_cast<int64_t>(t->maxSamples),
                             t->d_gate));
         VJ_LAUNCH_CHECK("refine_kernel");
     }
     VJ_TIMED_LAUNCH("finalize_kernel", s,
                     finalize_kernel<<<1, 32, 0, s>>>(t->d_feat, t->d_sumT, t->d_invNorm, n, t->d_ord, t->ordStride,
-                                                     sb, t->d_prm, t->d_refParity, t->d_refSplit, d_out, t->d_gate));
+                                                     sb, t->laneRun, t->d_prm, t->d_refParity, t->d_refSplit, d_out,
+                                                     t->d_gate));
     VJ_LAUNCH_CHECK("finalize_kernel");
     return ok();
 }
@@ -1497,7 +1526,7 @@ int vj_trainer_sort_per_feature(vj_trainer* t, const float* d_resp, int featureC
     if (!t || !d_resp || !d_sortedIdx || featureCount <= 0 || t->n <= 0)
         return set_error(VJ_INVALID_ARG, "vj_trainer_sort_per_feature: bad arguments");
     const int st = launch_eval_sort(nullptr, 0, featureCount, nullptr, nullptr, t->n, d_resp, d_sortedIdx, t->n,
-                                    false, nullptr, 0, 0, static_cast<cudaStream_t>(stream));
+                                    false, nullptr, 0, 0, 16, static_cast<cudaStream_t>(stream));
     return st == VJ_OK ? ok() : st;
 }
 
