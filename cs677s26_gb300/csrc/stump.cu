@@ -113,10 +113,22 @@ __host__ __device__ __forceinline__ uint32_t slot_sample(uint32_t v, int slotBas
 // Fills a block's shared weights: one copy, or both copies when slotBase > 0,
 // and the zero slot.
 __device__ __forceinline__ void fill_weights(float* dst, const float* __restrict__ src, int n, int slotBase) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float w = src[i];
-        dst[i] = w;
-        if (slotBase > 0) dst[slotBase + copy1_offset(i)] = w;
+    // eight loads in flight per thread
+    for (int i0 = threadIdx.x; i0 < n; i0 += 8 * blockDim.x) {
+        float w[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = i0 + u * static_cast<int>(blockDim.x);
+            w[u] = i < n ? __ldg(src + i) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = i0 + u * static_cast<int>(blockDim.x);
+            if (i < n) {
+                dst[i] = w[u];
+                if (slotBase > 0) dst[slotBase + copy1_offset(i)] = w[u];
+            }
+        }
     }
     if (threadIdx.x == 0) dst[zero_slot(n, slotBase)] = 0.0f;
 }
@@ -600,6 +612,7 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
               unsigned long long* __restrict__ candKey, float2* __restrict__ prefix, int64_t prefixStride,
               const int* gate) {
     if (gate_closed(gate)) return;
+    if (static_cast<int>(blockIdx.x) * kRefineWarps >= prm->ncand) return;  // no candidate in this block
     extern __shared__ float wsgS[];
     // per warp and chunk position: first the (positive, negative) addends of
     // the position's sample, then, in place, the left sums after it
@@ -689,16 +702,29 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
         // the float bits order like the values and the triple packs into one
         // key.
         unsigned long long best = ~0ull;
-        for (int base = 0; base < n - 1; base += 256) {
+        // the 8 split bits of positions k0..k0+7 (one lane run, one bitmask
+        // word) and the left sums at the valid ones; issued a chunk ahead
+        auto sload = [&](int base, float2 (&lv)[8]) -> uint32_t {
             const int k0 = base + lane * 8;
-            // the 8 split bits of positions k0..k0+7 (one lane run, one bitmask word)
-            const int l = k0 / L, r = k0 - l * L;
-            const uint32_t g =
-                (k0 < n - 1) ? (static_cast<uint32_t>(__ldg(grow + (r >> 4) * 32 + l)) >> (r & 15)) & 0xFFu : 0u;  // gap_word
+            uint32_t g = 0;
+            if (k0 < n - 1) {
+                const int l = k0 / L, r = k0 - l * L;
+                g = (static_cast<uint32_t>(__ldg(grow + (r >> 4) * 32 + l)) >> (r & 15)) & 0xFFu;  // gap_word
+            }
+#pragma unroll
+            for (int h = 0; h < 8; ++h) lv[h] = ((g >> h) & 1u) ? prow[k0 + h] : make_float2(0.0f, 0.0f);
+            return g;
+        };
+        float2 lc[8];
+        uint32_t gc = sload(0, lc);
+        for (int base = 0; base < n - 1; base += 256) {
+            float2 ln[8];
+            const uint32_t gn = sload(base + 256, ln);
+            const int k0 = base + lane * 8;
 #pragma unroll
             for (int h = 0; h < 8; ++h) {
-                if ((g >> h) & 1u) {
-                    const float2 l = prow[k0 + h];
+                if ((gc >> h) & 1u) {
+                    const float2 l = lc[h];
                     const float eL = __fadd_rn(l.y, __fsub_rn(tp, l.x));  // parity -1
                     const float eR = __fadd_rn(l.x, __fsub_rn(tn, l.y));  // parity +1
                     const unsigned k = static_cast<unsigned>(k0 + h);
@@ -708,6 +734,9 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
                     best = min(best, min(kL, kR));
                 }
             }
+#pragma unroll
+            for (int h = 0; h < 8; ++h) lc[h] = ln[h];
+            gc = gn;
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
