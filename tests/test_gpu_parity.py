@@ -122,11 +122,12 @@ def test_weak_search_resident_equals_fused(cuda, vj, oracle, gin, basic_pool):
     assert T.search() == fused
 
 
-@pytest.mark.parametrize("n", [24576, 25600])
+@pytest.mark.parametrize("n", [24576, 25600, 32768])
 def test_weak_search_both_weight_layouts(cuda, vj, oracle, basic_pool, n):
     """Up to 24,576 samples the resident orders carry slots of two bank-spread
-    weight copies; above that one copy and plain sample indices.  Both give the
-    oracle's pick, round after round."""
+    weight copies; above that one copy and plain sample indices, up to the
+    on-chip sort's maximum of 32,768.  All give the oracle's pick, round after
+    round."""
     p = vj.synth_patches(31, n // 2, n // 2)
     labels = np.array([1] * (n // 2) + [-1] * (n // 2), np.int8)
     feats = np.ascontiguousarray(basic_pool[::317][:512])
