@@ -60,6 +60,14 @@ constexpr float kU = 5.9604645e-08f;    // 2^-24, unit roundoff of FP32
 // The round update closes it with 2 when the search found no valid stump, the
 // calibration with 1 when the stage meets its targets, so a host can queue a
 // stage's rounds without reading anything back between them.
+// prmt.b32 whose selector nibbles have bit 3 set: each result byte is the
+// top bit of the selected source byte, replicated over the byte.
+__device__ __forceinline__ uint32_t prmt_sign(uint32_t a, uint32_t sel) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(0u), "r"(sel));
+    return r;
+}
+
 __device__ __forceinline__ bool gate_closed(const int* g) {
     return g != nullptr && *reinterpret_cast<const volatile int*>(g) != 0;
 }
@@ -235,12 +243,18 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
 #pragma unroll
             for (int j = 0; j < R; ++j) {
                 const uint32_t d = __byte_perm(dig[j >> 2], 0u, 0x4440u | static_cast<uint32_t>(j & 3));
-                // lanes whose digit differs in some bit: ballot XOR the lane's own bit, sign-extended
+                // lanes whose digit differs in some bit: ballot XOR the lane's own
+                // bit as an all-ones or all-zero mask.  Byte k of lo (hi) has bit k
+                // (4 + k) of the digit as its top bit (the four shifted copies of
+                // the nibble occupy disjoint bits), and prmt_sign spreads that bit
+                // over the word.
                 uint32_t differ = 0;
+                const uint32_t lo = (d & 0xFu) * 0x10204080u, hi = (d >> 4) * 0x10204080u;
 #pragma unroll
                 for (int b = 0; b < 8; ++b) {
-                    const uint32_t m = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-                    differ |= m ^ (0u - ((d >> b) & 1u));
+                    const uint32_t own = prmt_sign(b < 4 ? lo : hi, (8u + (b & 3)) * 0x1111u);
+                    const uint32_t m = __ballot_sync(0xffffffffu, own != 0u);
+                    differ |= m ^ own;
                 }
                 const uint32_t peers = ~differ;
                 // every lane reads its digit's counter; once the warp has read,
