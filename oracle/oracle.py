@@ -8,6 +8,7 @@ does.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -41,9 +42,14 @@ _lib = None
 _ref = None
 
 
-def build() -> None:
-    """Builds liboracle.so (and the reference harness when its sources exist)."""
-    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+def build(ref_src: str | None = None) -> None:
+    """Builds liboracle.so, and the reference harness when `ref_src` (or the
+    environment's REF) names the reference checkout."""
+    cmd = ["make", "-s", "-C", str(HERE)]
+    ref_src = ref_src or os.environ.get("REF")
+    if ref_src:
+        cmd.append(f"REF={ref_src}")
+    subprocess.run(cmd, check=True)
 
 
 def lib() -> C.CDLL:
@@ -61,6 +67,10 @@ def lib() -> C.CDLL:
         L.vjo_train_response.argtypes = [vp, vp, f32]
         L.vjo_weak_search.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, C.POINTER(Best), vp]
         L.vjo_feature_err64.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, vp]
+        L.vjo_sorted_build.restype = vp
+        L.vjo_sorted_build.argtypes = [vp, i32, vp, vp, i32, i32]
+        L.vjo_sorted_search.argtypes = [vp, vp, vp, vp, vp, i32, C.POINTER(Best), vp]
+        L.vjo_sorted_free.argtypes = [vp]
         L.vjo_round_update.argtypes = [vp, C.POINTER(Best), vp, vp, vp, vp, vp, vp, i32, vp]
         L.vjo_stage_calibrate.argtypes = [vp, vp, i32, i32, f32, f32, i32, vp, vp]
         L.vjo_resize.argtypes = [vp, i32, i32, i32, vp, i32, i32]
@@ -73,6 +83,12 @@ def lib() -> C.CDLL:
         L.vjo_group_first_order.argtypes = [vp, i32, i32, f32, vp]
         L.vjo_crop_resize.restype = None
         L.vjo_crop_resize.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp]
+        L.vjo_synth_patches.restype = None
+        L.vjo_synth_patches.argtypes = [C.c_uint64, i32, i32, vp]
+        L.vjo_synth_scene.restype = i32
+        L.vjo_synth_scene.argtypes = [C.c_uint64, i32, i32, i32, i32, i32, vp]
+        L.vjo_synth_cascade.restype = i32
+        L.vjo_synth_cascade.argtypes = [C.c_uint64, i32, i32, vp, vp]
         _lib = L
     return _lib
 
@@ -141,6 +157,37 @@ def weak_search(feats, sums, inv, labels, weights, active=None, used=None, threa
     return (b.as_dict(), per) if per_feature else b.as_dict()
 
 
+class SortedPool:
+    """Stage-resident form of weak_search: every feature of `feats` sorted once
+    (6 bytes of host memory per feature-sample), then search() per round with
+    the same sweep and pick rule as weak_search."""
+
+    def __init__(self, feats, sums, inv, threads=8):
+        self.feats = np.ascontiguousarray(feats)
+        self.n = len(inv)
+        self.h = lib().vjo_sorted_build(_p(self.feats), len(self.feats), _p(sums), _p(inv), self.n, threads)
+        if not self.h:
+            raise MemoryError("vjo_sorted_build: out of host memory")
+
+    def search(self, labels, weights, active=None, used=None, threads=8, per_feature=False):
+        b = Best()
+        per = np.zeros(len(self.feats), dtype=BEST) if per_feature else None
+        lib().vjo_sorted_search(self.h, _p(used), _p(labels), _p(active), _p(weights), threads, C.byref(b),
+                                _p(per))
+        return (b.as_dict(), per) if per_feature else b.as_dict()
+
+    def close(self):
+        if self.h:
+            lib().vjo_sorted_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # interpreter shutdown
+            pass
+
+
 def feature_err64(feats, sums, inv, labels, weights, active=None, used=None, threads=8):
     out = np.zeros(len(feats), dtype=np.float64)
     lib().vjo_feature_err64(_p(feats), len(feats), _p(used), _p(sums), _p(inv), _p(labels), _p(active),
@@ -205,3 +252,26 @@ def crop_resize(img, box, out=24):
     x, y, w, h = (int(v) for v in box)
     lib().vjo_crop_resize(_p(img), img.shape[1], img.shape[0], img.shape[1], x, y, w, h, out, _p(dst))
     return dst
+
+
+def synth_patches(seed: int, n_pos: int, n_neg: int) -> np.ndarray:
+    """n_pos face patterns then n_neg texture patches, (n, 24, 24) uint8."""
+    out = np.zeros((n_pos + n_neg, 24, 24), np.uint8)
+    lib().vjo_synth_patches(seed, n_pos, n_neg, _p(out))
+    return out
+
+
+def synth_scene(seed: int, w: int, h: int, n_paste: int, min_size: int = 24, max_size: int = 300) -> np.ndarray:
+    out = np.zeros((h, w), np.uint8)
+    if lib().vjo_synth_scene(seed, w, h, n_paste, min_size, max_size, _p(out)) != 0:
+        raise ValueError("synth_scene: bad arguments")
+    return out
+
+
+def synth_cascade(seed: int, stages: int = 38, stumps: int = 6061):
+    """(stumps, stages) of the synthetic cascade over the Basic pool."""
+    st = np.zeros(stumps, STUMP)
+    sg = np.zeros(stages, STAGE)
+    if lib().vjo_synth_cascade(seed, stages, stumps, _p(st), _p(sg)) != 0:
+        raise ValueError("synth_cascade: bad arguments")
+    return st, sg

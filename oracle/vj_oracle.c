@@ -222,20 +222,6 @@ static void kv_sort(kv* a, kv* tmp, int n) {
     }
 }
 
-typedef struct {
-    const vjo_feature* feats;
-    const uint8_t* usedMask;
-    const uint32_t* sums;
-    const float* invNorm;
-    const int8_t* labels;
-    const uint8_t* active;
-    const float* weights;
-    int n;
-    int f0, f1;
-    vjo_best* per;     /* per-feature best, CPU semantics */
-    double* err64;     /* per-feature FP64 best (may be NULL) */
-} search_job;
-
 /* The CPU search's update rule (main.cu:660-677) for candidates of one
  * feature: lower err wins; at equal err parity +1 replaces parity -1. */
 static void consider(vjo_best* b, float err, int parity, int k, float theta) {
@@ -247,73 +233,142 @@ static void consider(vjo_best* b, float err, int parity, int k, float theta) {
     }
 }
 
+/* Sorted responses of one feature: v[k] and the sample ix[k] at sorted
+ * position k (the stable_sort of main.cu:612-624). */
+static void sort_feature(const vjo_feature* f, const uint32_t* sums, const float* invNorm, int n, kv* a, kv* t,
+                         float* v, uint16_t* ix) {
+    for (int i = 0; i < n; ++i) {
+        a[i].v = vjo_train_response(f, sums + (size_t)i * 625, invNorm[i]);
+        a[i].i = (uint16_t)i;
+    }
+    kv_sort(a, t, n);
+    for (int k = 0; k < n; ++k) {
+        v[k] = a[k].v;
+        ix[k] = a[k].i;
+    }
+}
+
+/* Threshold sweep of one feature over its sorted samples, main.cu:626-678:
+ * sequential FP32 totals over the sorted order (inactive samples skipped),
+ * then the sequential left sums and, at every valid split
+ * (v[k] + 1e-7f < v[k+1]), both parities' errors.  b arrives with
+ * featureIdx set and err = +inf; *best64 receives the feature's smallest FP64
+ * error over its valid splits and b->err64 the FP64 error of the chosen one. */
+static void sweep_feature(const float* v, const uint16_t* ix, int n, const int8_t* labels, const uint8_t* active,
+                          const float* weights, vjo_best* b, double* best64) {
+    float tp = 0.0f, tn = 0.0f;
+    double tp64 = 0.0, tn64 = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const int s = ix[k];
+        if (active && active[s] == 0) continue;
+        if (labels[s] > 0) {
+            tp += weights[s];
+            tp64 += (double)weights[s];
+        } else {
+            tn += weights[s];
+            tn64 += (double)weights[s];
+        }
+    }
+    float lp = 0.0f, ln = 0.0f;
+    double lp64 = 0.0, ln64 = 0.0, m64 = INFINITY;
+    for (int k = 0; k + 1 < n; ++k) {
+        const int s = ix[k];
+        if (!active || active[s] != 0) {
+            if (labels[s] > 0) {
+                lp += weights[s];
+                lp64 += (double)weights[s];
+            } else {
+                ln += weights[s];
+                ln64 += (double)weights[s];
+            }
+        }
+        const float v0 = v[k], v1 = v[k + 1];
+        if (!(v0 + 1e-7f < v1)) continue;
+        const float rp = tp - lp, rn = tn - ln;
+        const float theta = 0.5f * (v0 + v1);
+        const float eL = ln + rp; /* left predicts +1: parity -1 */
+        consider(b, eL, -1, k, theta);
+        const float eR = lp + rn; /* left predicts -1: parity +1 */
+        consider(b, eR, +1, k, theta);
+        const double e1 = ln64 + (tp64 - lp64), e2 = lp64 + (tn64 - ln64);
+        if (e1 < m64) m64 = e1;
+        if (e2 < m64) m64 = e2;
+        if (k == b->split) b->err64 = (b->parity < 0) ? e1 : e2;
+    }
+    *best64 = m64;
+}
+
+static vjo_best no_split(int f) {
+    vjo_best b;
+    b.featureIdx = f;
+    b.err = INFINITY;
+    b.theta = 0.0f;
+    b.parity = 1;
+    b.split = -1;
+    b.err64 = INFINITY;
+    return b;
+}
+
+/* A pool's per-feature sorted responses, kept for a stage (see
+ * vjo_sorted_build): row f holds v[f][k] and ix[f][k]. */
+struct vjo_sorted {
+    int nFeat, n;
+    float* v;
+    uint16_t* ix;
+};
+
+typedef struct {
+    const vjo_feature* feats;
+    const uint8_t* usedMask;
+    const uint32_t* sums;
+    const float* invNorm;
+    const int8_t* labels;
+    const uint8_t* active;
+    const float* weights;
+    int n;
+    int f0, f1;
+    vjo_best* per;           /* per-feature best, CPU semantics */
+    double* err64;           /* per-feature FP64 best (may be NULL) */
+    const vjo_sorted* sorted; /* sweep stored orders instead of sorting */
+    vjo_sorted* build;       /* fill these rows instead of sweeping */
+} search_job;
+
 static void* search_worker(void* arg) {
     search_job* J = (search_job*)arg;
     const int n = J->n;
     kv* a = (kv*)malloc(sizeof(kv) * (size_t)n);
     kv* t = (kv*)malloc(sizeof(kv) * (size_t)n);
+    float* v = (float*)malloc(sizeof(float) * (size_t)n);
+    uint16_t* ix = (uint16_t*)malloc(sizeof(uint16_t) * (size_t)n);
     for (int f = J->f0; f < J->f1; ++f) {
-        vjo_best b;
-        b.featureIdx = f;
-        b.err = INFINITY;
-        b.theta = 0.0f;
-        b.parity = 1;
-        b.split = -1;
-        b.err64 = INFINITY;
+        if (J->build) {
+            sort_feature(&J->feats[f], J->sums, J->invNorm, n, a, t, J->build->v + (size_t)f * n,
+                         J->build->ix + (size_t)f * n);
+            continue;
+        }
+        vjo_best b = no_split(f);
         if (J->usedMask && J->usedMask[f]) {
             J->per[f] = b;
             if (J->err64) J->err64[f] = INFINITY;
             continue;
         }
-        for (int i = 0; i < n; ++i) {
-            a[i].v = vjo_train_response(&J->feats[f], J->sums + (size_t)i * 625, J->invNorm[i]);
-            a[i].i = (uint16_t)i;
+        const float* fv = v;
+        const uint16_t* fix = ix;
+        if (J->sorted) {
+            fv = J->sorted->v + (size_t)f * n;
+            fix = J->sorted->ix + (size_t)f * n;
+        } else {
+            sort_feature(&J->feats[f], J->sums, J->invNorm, n, a, t, v, ix);
         }
-        kv_sort(a, t, n);
-        float tp = 0.0f, tn = 0.0f;
-        double tp64 = 0.0, tn64 = 0.0;
-        for (int k = 0; k < n; ++k) {
-            const int s = a[k].i;
-            if (J->active && J->active[s] == 0) continue;
-            if (J->labels[s] > 0) {
-                tp += J->weights[s];
-                tp64 += (double)J->weights[s];
-            } else {
-                tn += J->weights[s];
-                tn64 += (double)J->weights[s];
-            }
-        }
-        float lp = 0.0f, ln = 0.0f;
-        double lp64 = 0.0, ln64 = 0.0, best64 = INFINITY;
-        for (int k = 0; k + 1 < n; ++k) {
-            const int s = a[k].i;
-            if (!J->active || J->active[s] != 0) {
-                if (J->labels[s] > 0) {
-                    lp += J->weights[s];
-                    lp64 += (double)J->weights[s];
-                } else {
-                    ln += J->weights[s];
-                    ln64 += (double)J->weights[s];
-                }
-            }
-            const float v0 = a[k].v, v1 = a[k + 1].v;
-            if (!(v0 + 1e-7f < v1)) continue;
-            const float rp = tp - lp, rn = tn - ln;
-            const float theta = 0.5f * (v0 + v1);
-            const float eL = ln + rp; /* left predicts +1: parity -1 */
-            consider(&b, eL, -1, k, theta);
-            const float eR = lp + rn; /* left predicts -1: parity +1 */
-            consider(&b, eR, +1, k, theta);
-            const double e1 = ln64 + (tp64 - lp64), e2 = lp64 + (tn64 - ln64);
-            if (e1 < best64) best64 = e1;
-            if (e2 < best64) best64 = e2;
-            if (k == b.split) b.err64 = (b.parity < 0) ? e1 : e2;
-        }
+        double m64;
+        sweep_feature(fv, fix, n, J->labels, J->active, J->weights, &b, &m64);
         J->per[f] = b;
-        if (J->err64) J->err64[f] = best64;
+        if (J->err64) J->err64[f] = m64;
     }
     free(a);
     free(t);
+    free(v);
+    free(ix);
     return NULL;
 }
 
@@ -342,26 +397,24 @@ static void run_search(search_job* base, int nFeat, int threads) {
         if (threads > 1 && tid[t]) pthread_join(tid[t], NULL);
 }
 
+/* Across features, in increasing featureIdx, only a strictly lower err
+ * replaces the current best (main.cu:660-662: featureIdx < best.featureIdx
+ * never holds for a later feature). */
+static vjo_best pick_across(const vjo_best* per, int nFeat) {
+    vjo_best g = no_split(-1);
+    for (int f = 0; f < nFeat; ++f)
+        if (per[f].split >= 0 && per[f].err < g.err) g = per[f];
+    return g;
+}
+
 void vjo_weak_search(const vjo_feature* feats, int nFeat, const uint8_t* usedMask,
                      const uint32_t* sums, const float* invNorm, const int8_t* labels,
                      const uint8_t* active, const float* weights, int n, int threads,
                      vjo_best* out, vjo_best* perFeature) {
     vjo_best* per = perFeature ? perFeature : (vjo_best*)malloc(sizeof(vjo_best) * (size_t)(nFeat > 0 ? nFeat : 1));
-    search_job J = {feats, usedMask, sums, invNorm, labels, active, weights, n, 0, 0, per, NULL};
+    search_job J = {feats, usedMask, sums, invNorm, labels, active, weights, n, 0, 0, per, NULL, NULL, NULL};
     run_search(&J, nFeat, threads);
-    /* Across features, in increasing featureIdx, only a strictly lower err
-     * replaces the current best (main.cu:660-662: featureIdx < best.featureIdx
-     * never holds for a later feature). */
-    vjo_best g;
-    g.featureIdx = -1;
-    g.err = INFINITY;
-    g.theta = 0.0f;
-    g.parity = 1;
-    g.split = -1;
-    g.err64 = INFINITY;
-    for (int f = 0; f < nFeat; ++f)
-        if (per[f].split >= 0 && per[f].err < g.err) g = per[f];
-    *out = g;
+    *out = pick_across(per, nFeat);
     if (!perFeature) free(per);
 }
 
@@ -370,9 +423,43 @@ void vjo_feature_err64(const vjo_feature* feats, int nFeat, const uint8_t* usedM
                        const uint8_t* active, const float* weights, int n, int threads,
                        double* err64) {
     vjo_best* per = (vjo_best*)malloc(sizeof(vjo_best) * (size_t)(nFeat > 0 ? nFeat : 1));
-    search_job J = {feats, usedMask, sums, invNorm, labels, active, weights, n, 0, 0, per, err64};
+    search_job J = {feats, usedMask, sums, invNorm, labels, active, weights, n, 0, 0, per, err64, NULL, NULL};
     run_search(&J, nFeat, threads);
     free(per);
+}
+
+vjo_sorted* vjo_sorted_build(const vjo_feature* feats, int nFeat, const uint32_t* sums, const float* invNorm,
+                             int n, int threads) {
+    vjo_sorted* s = (vjo_sorted*)calloc(1, sizeof(vjo_sorted));
+    if (!s) return NULL;
+    s->nFeat = nFeat;
+    s->n = n;
+    s->v = (float*)malloc(sizeof(float) * (size_t)nFeat * (size_t)n);
+    s->ix = (uint16_t*)malloc(sizeof(uint16_t) * (size_t)nFeat * (size_t)n);
+    if (!s->v || !s->ix) {
+        vjo_sorted_free(s);
+        return NULL;
+    }
+    search_job J = {feats, NULL, sums, invNorm, NULL, NULL, NULL, n, 0, 0, NULL, NULL, NULL, s};
+    run_search(&J, nFeat, threads);
+    return s;
+}
+
+void vjo_sorted_search(const vjo_sorted* s, const uint8_t* usedMask, const int8_t* labels, const uint8_t* active,
+                       const float* weights, int threads, vjo_best* out, vjo_best* perFeature) {
+    const int nFeat = s->nFeat;
+    vjo_best* per = perFeature ? perFeature : (vjo_best*)malloc(sizeof(vjo_best) * (size_t)(nFeat > 0 ? nFeat : 1));
+    search_job J = {NULL, usedMask, NULL, NULL, labels, active, weights, s->n, 0, 0, per, NULL, s, NULL};
+    run_search(&J, nFeat, threads);
+    *out = pick_across(per, nFeat);
+    if (!perFeature) free(per);
+}
+
+void vjo_sorted_free(vjo_sorted* s) {
+    if (!s) return;
+    free(s->v);
+    free(s->ix);
+    free(s);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -65,6 +65,19 @@ void vjo_weak_search(const vjo_feature* feats, int nFeat, const uint8_t* usedMas
                      const uint8_t* active, const float* weights, int n, int threads,
                      vjo_best* out, vjo_best* perFeature);
 
+/* Stage-resident form of vjo_weak_search.  Within a stage the responses and
+ * hence every feature's sorted order stay fixed; only the weights change.
+ * vjo_sorted_build sorts every feature of the pool once (6 bytes per
+ * feature-sample of host memory), and vjo_sorted_search then runs the same
+ * sweep and the same cross-feature rule as vjo_weak_search over the stored
+ * orders, so its result equals vjo_weak_search's on the same inputs. */
+typedef struct vjo_sorted vjo_sorted;
+vjo_sorted* vjo_sorted_build(const vjo_feature* feats, int nFeat, const uint32_t* sums, const float* invNorm,
+                             int n, int threads);
+void vjo_sorted_search(const vjo_sorted* s, const uint8_t* usedMask, const int8_t* labels, const uint8_t* active,
+                       const float* weights, int threads, vjo_best* out, vjo_best* perFeature);
+void vjo_sorted_free(vjo_sorted* s);
+
 /* FP64 weighted error of every feature's best split (exact-sum reference for
  * the per-round error statement).  err64[f] = +inf when the feature has no
  * valid split or is masked. */
@@ -118,6 +131,15 @@ void vjo_crop_resize(const uint8_t* img, int w, int h, int stride, int x, int y,
 /* vjo_group with the output ordered by each cluster's first member (smallest
  * input index). */
 int vjo_group_first_order(const vjo_det* in, int n, int minNeighbors, float eps, vjo_det* out);
+
+/* Seeded synthetic inputs (vj_synth.c), byte-identical to the package's
+ * generators: nPos face patterns then nNeg texture patches of 24x24; a
+ * texture scene with nPaste faces at log-uniform sizes (returns 0, or -1 on
+ * bad arguments); a cascade of stageCount stages and totalStumps stumps over
+ * the Basic pool (returns 0 or -1). */
+void vjo_synth_patches(uint64_t seed, int nPos, int nNeg, uint8_t* out);
+int vjo_synth_scene(uint64_t seed, int w, int h, int nPaste, int minSize, int maxSize, uint8_t* out);
+int vjo_synth_cascade(uint64_t seed, int stageCount, int totalStumps, vjo_stump* stumps, vjo_stage* stages);
 
 #ifdef __cplusplus
 }
