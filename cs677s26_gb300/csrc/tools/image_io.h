@@ -21,61 +21,91 @@ struct Gray {
     std::vector<uint8_t> px;
 };
 
-// Next header token, skipping whitespace and '#' comment lines.
-inline bool next_token(std::istream& is, std::string& tok) {
-    tok.clear();
-    while (is.good()) {
-        const int c = is.peek();
-        if (c == '#') {
-            std::string line;
-            std::getline(is, line);
-            continue;
-        }
-        if (c != EOF && std::isspace(static_cast<unsigned char>(c))) {
-            is.get();
-            continue;
-        }
-        break;
+// Whole-file read in 1 MiB pieces.  0: ok, 1: cannot open, 2: read error.
+inline int read_file(const std::string& path, std::vector<uint8_t>& bytes) {
+    bytes.clear();
+    std::FILE* fp = std::fopen(path.c_str(), "rb");
+    if (!fp) return 1;
+    constexpr size_t kPiece = 1u << 20;
+    size_t got = 0;
+    for (;;) {
+        bytes.resize(got + kPiece);
+        const size_t r = std::fread(bytes.data() + got, 1, kPiece, fp);
+        got += r;
+        if (r < kPiece) break;
     }
-    if (!is.good()) return false;
-    is >> tok;
-    return !tok.empty();
+    const bool bad = std::ferror(fp) != 0;
+    std::fclose(fp);
+    bytes.resize(got);
+    return bad ? 2 : 0;
 }
 
-// Binary P5 PGM with maxval <= 255 (loadPGM, main.cu:315-354).
+// Netpbm P5 header reader over a byte buffer: fields are separated by
+// whitespace, and a '#' starts a comment that runs to the end of its line.
+struct PnmHeader {
+    const std::vector<uint8_t>& b;
+    size_t at = 0;
+    static bool space(uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
+    void skip() {
+        while (at < b.size()) {
+            if (b[at] == '#') {
+                while (at < b.size() && b[at] != '\n') ++at;
+            } else if (space(b[at])) {
+                ++at;
+            } else {
+                break;
+            }
+        }
+    }
+    // A decimal field; false when it is missing, not a number or above 2^30.
+    bool number(int& v) {
+        skip();
+        int64_t acc = 0;
+        const size_t from = at;
+        while (at < b.size() && b[at] >= '0' && b[at] <= '9') {
+            acc = acc * 10 + (b[at++] - '0');
+            if (acc > (1 << 30)) return false;
+        }
+        if (at == from) return false;
+        v = static_cast<int>(acc);
+        return true;
+    }
+};
+
+// Binary P5 PGM with maxval <= 255 (the reference's loadPGM, main.cu:315-354,
+// accepts the same files and prints the same messages).
 inline bool load_pgm(const std::string& path, Gray& g, bool quiet = false) {
-    std::ifstream ifs(path, std::ios::binary);
-    if (!ifs) {
+    std::vector<uint8_t> bytes;
+    if (read_file(path, bytes) == 1) {
         if (!quiet) std::cerr << "[ERR] Cannot open PGM: " << path << "\n";
         return false;
     }
-    std::string tok;
-    if (!next_token(ifs, tok) || tok != "P5") {
+    PnmHeader hdr{bytes};
+    hdr.skip();
+    const bool magic = hdr.at + 2 <= bytes.size() && bytes[hdr.at] == 'P' && bytes[hdr.at + 1] == '5' &&
+                       (hdr.at + 2 == bytes.size() || PnmHeader::space(bytes[hdr.at + 2]) || bytes[hdr.at + 2] == '#');
+    if (!magic) {
         if (!quiet) std::cerr << "[ERR] Unsupported PGM format (need P5): " << path << "\n";
         return false;
     }
-    int maxVal = 0;
-    try {
-        if (!next_token(ifs, tok)) return false;
-        g.w = std::stoi(tok);
-        if (!next_token(ifs, tok)) return false;
-        g.h = std::stoi(tok);
-        if (!next_token(ifs, tok)) return false;
-        maxVal = std::stoi(tok);
-    } catch (...) {
+    hdr.at += 2;
+    int w = 0, h = 0, maxVal = 0;
+    if (!hdr.number(w) || !hdr.number(h) || !hdr.number(maxVal) || w <= 0 || h <= 0 || maxVal <= 0 ||
+        maxVal > 255) {
         if (!quiet) std::cerr << "[ERR] Invalid PGM metadata\n";
         return false;
     }
-    if (g.w <= 0 || g.h <= 0 || maxVal <= 0 || maxVal > 255) {
-        if (!quiet) std::cerr << "[ERR] Invalid PGM metadata\n";
-        return false;
-    }
-    ifs.get();  // the single whitespace after the header
-    g.px.resize(static_cast<size_t>(g.w) * g.h);
-    if (!ifs.read(reinterpret_cast<char*>(g.px.data()), static_cast<std::streamsize>(g.px.size()))) {
+    // exactly one whitespace byte separates the header from the raster
+    const size_t raster = hdr.at + 1;
+    const size_t need = static_cast<size_t>(w) * static_cast<size_t>(h);
+    if (raster > bytes.size() || bytes.size() - raster < need) {
         if (!quiet) std::cerr << "[ERR] Failed to read PGM pixel payload\n";
         return false;
     }
+    g.w = w;
+    g.h = h;
+    g.px.assign(bytes.begin() + static_cast<std::ptrdiff_t>(raster),
+                bytes.begin() + static_cast<std::ptrdiff_t>(raster + need));
     return true;
 }
 

@@ -68,29 +68,29 @@ constexpr int kPerImageKeep = 256;
 constexpr int kMiningMax = 2048;
 constexpr int kRoundChunk = 16;  // boosting rounds queued per read of the stage gate
 
+// A raw sample file: N patches of 24x24 uint8 back to back, N from the file
+// size (the reference's loadRawSampleBin, main.cu:122-162, reads the same
+// format and prints the same messages).
 bool load_raw_bin(const std::string& path, std::vector<uint8_t>& out, int& count) {
-    std::ifstream ifs(path, std::ios::binary);
-    if (!ifs) {
-        std::cerr << "[ERR] Cannot open: " << path << "\n";
-        return false;
+    switch (vjtools::read_file(path, out)) {
+        case 1:
+            std::cerr << "[ERR] Cannot open: " << path << "\n";
+            return false;
+        case 2:
+            std::cerr << "[ERR] Failed to read: " << path << "\n";
+            return false;
+        default:
+            break;
     }
-    ifs.seekg(0, std::ios::end);
-    const std::streamoff sz = ifs.tellg();
-    ifs.seekg(0, std::ios::beg);
-    if (sz <= 0) {
+    if (out.empty()) {
         std::cerr << "[ERR] Empty file: " << path << "\n";
         return false;
     }
-    if (sz % kPix != 0) {
+    if (out.size() % kPix != 0) {
         std::cerr << "[ERR] File size is not divisible by samplePixels: " << path << "\n";
         return false;
     }
-    out.resize(static_cast<size_t>(sz));
-    if (!ifs.read(reinterpret_cast<char*>(out.data()), sz)) {
-        std::cerr << "[ERR] Failed to read: " << path << "\n";
-        return false;
-    }
-    count = static_cast<int>(sz / kPix);
+    count = static_cast<int>(out.size() / kPix);
     return true;
 }
 
