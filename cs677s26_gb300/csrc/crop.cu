@@ -90,7 +90,11 @@ int vj_crop_resize_batch(int nImages, const uint8_t* const* images, const int* w
     cudaError_t e = cudaMemcpyAsync(dj, jobs.data(), sizeof(CropJob) * jobs.size(), cudaMemcpyHostToDevice, s);
     const int64_t total = static_cast<int64_t>(nCrops) * outSize * outSize;
     if (e == cudaSuccess) {
-        const int64_t blocks = std::min<int64_t>((total + 255) / 256, int64_t(152) * 16);
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        // grid-stride loop: at most 16 blocks of 256 threads per SM of this device
+        const int64_t blocks = std::min<int64_t>((total + 255) / 256, int64_t(sms > 0 ? sms : 1) * 16);
         crop_resize_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(dj, total, outSize, d_out);
         e = cudaGetLastError();
     }

@@ -22,6 +22,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // CUcontext / CUresult types only; the driver is reached through the runtime
+
 #include "integral_dev.cuh"
 
 namespace vjgb {
@@ -238,24 +240,62 @@ __global__ void store_job_kernel(IIJob* dst, IIJob job) { *dst = job; }
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
-unsigned char* g_noalloc_ptr[kMaxDevices] = {};
+struct NoAllocSlot {
+    unsigned long long ctx = 0;  // unique id of the context the address belongs to
+    unsigned char* ptr = nullptr;
+};
+NoAllocSlot g_noalloc_slot[kMaxDevices];
 
-// Device address of the scratch array on the current device (looked up once
-// per device, with that device current).
+// Unique id of the calling thread's current context, or 0 when it has none.
+// cuCtxGetCurrent / cuCtxGetId are reached through the runtime's driver entry
+// points, so the library does not link the driver library itself.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent getCurrent = nullptr;
+    static GetId getId = nullptr;
+    static bool resolved = false;
+    if (!resolved) {  // under g_noalloc_mu
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess)
+            getCurrent = reinterpret_cast<GetCurrent>(a);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qb == cudaDriverEntryPointSuccess)
+            getId = reinterpret_cast<GetId>(b);
+        resolved = true;
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!getCurrent || !getId || getCurrent(&c) != CUDA_SUCCESS || !c || getId(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array in the current context.  The address
+// belongs to the context that loaded the module: after cudaDeviceReset, or a
+// primary context released and created again, the module loads again and the
+// array may move.  So the address is cached per device together with the
+// unique id of the context it was taken in, and looked up again (with that
+// device current) whenever the current context differs.
 int noalloc_scratch(unsigned char** out) {
     int dev = 0;
     VJ_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return set_error(VJ_RUNTIME_ERROR, "vj_integral_image_noalloc: device id");
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoAllocSlot& slot = g_noalloc_slot[dev];
+    const unsigned long long ctx = current_context_id();
+    if (!slot.ptr || ctx == 0 || slot.ctx != ctx) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return set_error(VJ_CUDA_ERROR, std::string("vj_integral_image_noalloc: cudaGetSymbolAddress: ") +
                                                 cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+        slot.ptr = static_cast<unsigned char*>(p);
+        slot.ctx = current_context_id();  // the lookup creates the primary context if there was none
     }
-    *out = g_noalloc_ptr[dev];
+    *out = slot.ptr;
     return VJ_OK;
 }
 

@@ -208,8 +208,10 @@ int vj_integral_image(const uint8_t* d_gray, int w, int h, int stride,
  * every GPU loading the library holds until the process exits.  Limits:
  * w <= 3840, h <= 2160, and d_sqsum must be given (there is no room for
  * temporary squared sums); larger inputs return VJ_INVALID_ARG.  The first
- * call on each device looks up the array's device address (cudaGetSymbolAddress),
- * so make that first call before any stream capture.  Every call shares the
+ * call on each device (and the first after that device's context was reset
+ * and created again) looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Every call shares the
  * one array: calls that overlap on the GPU (different streams, or different
  * host threads) race and corrupt each other's results; keep them on one
  * stream.  Asynchronous on `stream`; results equal vj_integral_image's. */
@@ -295,6 +297,23 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
  * orders resident on the device (2 B per feature-sample) for the rounds of
  * the current stage.  Invalidated by vj_trainer_bind. */
 int vj_trainer_prepare_stage(vj_trainer* t, void* stream);
+
+/* Restricts vj_trainer_prepare_stage and vj_stump_search to the features
+ * [featureBegin, featureBegin + featureCount) of the pool: one feature tile
+ * of the reference's round loop (main.cu:2013-2053, the begin/count of each
+ * evaluateFeatureResponses .. selectBestInTile pass), kept for every round.
+ * The search's featureIdx and the used mask stay indexed by the whole pool,
+ * and vj_round_update still applies any feature of the pool, so ranks that
+ * each own one range exchange their 16-byte candidates, reduce them with
+ * vj_reduce_tile_best and apply the same update.  Setting a new pool resets
+ * the range to the whole pool; changing it invalidates prepared orders. */
+int vj_trainer_set_search_range(vj_trainer* t, int64_t featureBegin, int64_t featureCount);
+
+/* ReduceTileBestCandidatesKernel (main.cu:991-1028): d_out = the best of
+ * count candidates (device arrays), lower FP32 error first, then lower
+ * featureIdx; a candidate with featureIdx -1 (no valid split) wins only when
+ * every candidate has none. */
+int vj_reduce_tile_best(const vj_tile_best* d_in, int count, vj_tile_best* d_out, void* stream);
 
 /* Statistics of the last vj_stump_search (no reference counterpart): the
  * fast-pass minimum error, the width of the candidate window, how many
