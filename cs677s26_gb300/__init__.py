@@ -392,6 +392,11 @@ class AdaBoostTrainer:
     def prepareStage(self, stream=None) -> int:
         return Status(_capi.status("vj_trainer_prepare_stage", self._h, _stream(stream)))
 
+    def setSearchRange(self, featureBegin: int, featureCount: int) -> int:
+        """Restrict prepareStage/bestWeak to one feature range of the pool (a
+        rank's tile); featureIdx and the used mask stay pool-indexed."""
+        return Status(_capi.status("vj_trainer_set_search_range", self._h, featureBegin, featureCount))
+
     def bestWeak(self, dUsedFeatureMask, dOut, stream=None) -> int:
         """One round's full search; dOut is a 16-byte device buffer (TileBestCandidate)."""
         return Status(_capi.status("vj_stump_search", self._h, ptr(dUsedFeatureMask), ptr(dOut),

@@ -98,6 +98,8 @@ SIGNATURES = {
     "vj_trainer_select_best_in_tile": (i32, [vp, vp, i32, i32, vp, vp, vp]),
     "vj_stump_search": (i32, [vp, vp, vp, vp]),
     "vj_trainer_prepare_stage": (i32, [vp, vp]),
+    "vj_trainer_set_search_range": (i32, [vp, i64, i64]),
+    "vj_reduce_tile_best": (i32, [vp, i32, vp, vp]),
     "vj_trainer_stage_bytes": (i32, [vp, i32, pi64]),
     "vj_trainer_last_round": (i32, [vp, vp]),
     "vj_round_update": (i32, [vp, vp, vp, vp, vp, vp]),

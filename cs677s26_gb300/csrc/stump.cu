@@ -151,6 +151,61 @@ struct RoundParams {
     int status;                  // 0 ok, 1 no valid split anywhere
 };
 
+// Mask of the lanes of the warp whose 8-bit digit equals this lane's, from 8
+// ballots (one per digit bit): the lanes whose digit differs in some bit are
+// the ballot XOR the lane's own bit as an all-ones or all-zero mask.  Byte k
+// of lo (hi) has bit k (4 + k) of the digit as its top bit (the four shifted
+// copies of the nibble occupy disjoint bits), and prmt_sign spreads that bit
+// over the word.
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d) {
+    uint32_t differ = 0;
+    const uint32_t lo = (d & 0xFu) * 0x10204080u, hi = (d >> 4) * 0x10204080u;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const uint32_t own = prmt_sign(b < 4 ? lo : hi, (8u + (b & 3)) * 0x1111u);
+        const uint32_t m = __ballot_sync(0xffffffffu, own != 0u);
+        differ |= m ^ own;
+    }
+    return ~differ;
+}
+
+// Exclusive scan, in place, of the 256 x 32 per-(digit, warp) counters in
+// (digit, warp) order; 1024 threads, thread t scans 8 counters of digit t / 4.
+__device__ __forceinline__ void scan_digit_counters(uint32_t* cnt, uint32_t* warpTot) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int d = tid >> 2, w0 = (tid & 3) * 8;
+    uint32_t v[8];
+    uint32_t run = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t t = cnt[d * kCntStride + w0 + i];
+        v[i] = run;
+        run += t;
+    }
+    uint32_t incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warpTot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t t = warpTot[lane];
+        uint32_t s = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        warpTot[lane] = s - t;
+    }
+    __syncthreads();
+    const uint32_t base = warpTot[warp] + incl - run;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) cnt[d * kCntStride + w0 + i] = base + v[i];
+}
+
 // ---------------------------------------------------------------------------
 // 1. Evaluate + on-chip stable radix sort of one feature per CTA.
 // ---------------------------------------------------------------------------
@@ -243,20 +298,7 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
 #pragma unroll
             for (int j = 0; j < R; ++j) {
                 const uint32_t d = __byte_perm(dig[j >> 2], 0u, 0x4440u | static_cast<uint32_t>(j & 3));
-                // lanes whose digit differs in some bit: ballot XOR the lane's own
-                // bit as an all-ones or all-zero mask.  Byte k of lo (hi) has bit k
-                // (4 + k) of the digit as its top bit (the four shifted copies of
-                // the nibble occupy disjoint bits), and prmt_sign spreads that bit
-                // over the word.
-                uint32_t differ = 0;
-                const uint32_t lo = (d & 0xFu) * 0x10204080u, hi = (d >> 4) * 0x10204080u;
-#pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    const uint32_t own = prmt_sign(b < 4 ? lo : hi, (8u + (b & 3)) * 0x1111u);
-                    const uint32_t m = __ballot_sync(0xffffffffu, own != 0u);
-                    differ |= m ^ own;
-                }
-                const uint32_t peers = ~differ;
+                const uint32_t peers = digit_peers(d);
                 // every lane reads its digit's counter; once the warp has read,
                 // the first lane of each equal-digit group stores the new count
                 const uint32_t before = peers & lanemask_lt();
@@ -271,40 +313,7 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                     packed[j] |= rank << 16;
             }
             __syncthreads();
-            // Exclusive scan of the counters in (digit, warp) order.
-            {
-                const int d = tid >> 2, w0 = (tid & 3) * 8;
-                uint32_t v[8];
-                uint32_t run = 0;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const uint32_t t = cnt[d * kCntStride + w0 + i];
-                    v[i] = run;
-                    run += t;
-                }
-                uint32_t incl = run;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += y;
-                }
-                if (lane == 31) warpTot[warp] = incl;
-                __syncthreads();
-                if (warp == 0) {
-                    const uint32_t t = warpTot[lane];
-                    uint32_t s = t;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-                        if (lane >= o) s += y;
-                    }
-                    warpTot[lane] = s - t;
-                }
-                __syncthreads();
-                const uint32_t base = warpTot[warp] + incl - run;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) cnt[d * kCntStride + w0 + i] = base + v[i];
-            }
+            scan_digit_counters(cnt, warpTot);
             __syncthreads();
 #pragma unroll
             for (int j = 0; j < R; ++j) {
@@ -376,6 +385,149 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
                 *reinterpret_cast<uint4*>(orow + ord_slot(k, L)) = *reinterpret_cast<const uint4*>(idx + k);
         } else {
             for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 1b. The same evaluate + stable LSD radix sort for 32,768 < n <= 65,535
+//     samples, which do not fit on chip.  Each CTA keeps its feature's keys
+//     and sample indices in a private global scratch (12 bytes per position:
+//     two key and two index buffers; about 0.8 MB per CTA at 65,536
+//     positions, so the scratch of all CTAs stays mostly in L2) and moves the
+//     keys with the indices, so every read of a pass is coalesced; the ranks
+//     among equal digits (2 bytes per position) stay in shared memory.  Items
+//     are warp-contiguous as in eval_sort_kernel (position
+//     warp * 32R + 32j + lane), ranks come from the same ballots, and the
+//     outputs (order, split bitmask, layouts) are the same.  Positions from n
+//     up to 1024R carry the largest key and sort last.
+// ---------------------------------------------------------------------------
+constexpr int kOnChipSortMax = 32768;
+constexpr int kLargeSortMaxR = 64;  // 65,536 positions per feature
+__host__ __device__ __forceinline__ int large_sort_r(int n) { return (n + 1023) / 1024; }
+inline size_t large_sort_smem_bytes(int R) {
+    return static_cast<size_t>(256 * kCntStride) * 4 + static_cast<size_t>(1024 * R) * 2;
+}
+
+template <bool kFromResp>
+__global__ void __launch_bounds__(kSortThreads, 1)
+eval_sort_large_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int featCount,
+                       const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm, int n,
+                       const float* __restrict__ resp, uint16_t* __restrict__ ordOut, int64_t ordStride,
+                       bool ordPadded, uint16_t* __restrict__ gapOut, int64_t gapStride, int L, int R,
+                       uint32_t* __restrict__ keyScratch, uint16_t* __restrict__ idxScratch) {
+    const int NP = 1024 * R;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem);           // digit counters; later the split-bit words
+    uint16_t* rankS = reinterpret_cast<uint16_t*>(cnt + 256 * kCntStride);  // rank among equal digits
+    __shared__ uint32_t warpTot[32];
+    __shared__ vj_haar_feature sfeat;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gapWords = (n + 31) >> 5;
+    uint32_t* keyA = keyScratch + static_cast<size_t>(blockIdx.x) * 2 * NP;
+    uint32_t* keyB = keyA + NP;
+    uint16_t* idxA = idxScratch + static_cast<size_t>(blockIdx.x) * 2 * NP;
+    uint16_t* idxB = idxA + NP;
+
+    for (int fl = blockIdx.x; fl < featCount; fl += gridDim.x) {
+        // radix keys in sample order
+        if (kFromResp) {
+            const float* row = resp + static_cast<size_t>(fl) * n;
+            for (int s = tid; s < NP; s += kSortThreads) keyA[s] = s < n ? radix_key(__float_as_uint(row[s])) : ~0u;
+        } else {
+            if (tid == 0) sfeat = feats[featBegin + fl];
+            __syncthreads();
+            const vj_haar_feature& f = sfeat;
+            for (int s0 = tid; s0 < NP; s0 += 4 * kSortThreads) {
+                float r[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int s = s0 + u * kSortThreads;
+                    r[u] = s < n ? train_response(f, sumT, n, s, __ldg(invNorm + s)) : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int s = s0 + u * kSortThreads;
+                    if (s < NP) keyA[s] = s < n ? radix_key(__float_as_uint(r[u])) : ~0u;
+                }
+            }
+        }
+        __syncthreads();
+
+        for (int pass = 0; pass < 4; ++pass) {
+            const int shift = pass * 8;
+            const uint32_t* ks = (pass & 1) ? keyB : keyA;
+            uint32_t* kd = (pass & 1) ? keyA : keyB;
+            const uint16_t* is = (pass & 1) ? idxB : idxA;
+            uint16_t* id = (pass & 1) ? idxA : idxB;
+            for (int i = tid; i < 256 * kCntStride; i += kSortThreads) cnt[i] = 0;
+            __syncthreads();
+            // ranks among equal digits, in sequence order (warp-contiguous items)
+#pragma unroll 4
+            for (int j = 0; j < R; ++j) {
+                const int p = warp * 32 * R + j * 32 + lane;
+                const uint32_t d = (ks[p] >> shift) & 255u;
+                const uint32_t peers = digit_peers(d);
+                const uint32_t before = peers & lanemask_lt();
+                const uint32_t old = cnt[d * kCntStride + warp];
+                __syncwarp();
+                if (before == 0) cnt[d * kCntStride + warp] = old + __popc(peers);
+                __syncwarp();
+                rankS[p] = static_cast<uint16_t>(old + __popc(before));
+            }
+            __syncthreads();
+            scan_digit_counters(cnt, warpTot);
+            __syncthreads();
+#pragma unroll 4
+            for (int j = 0; j < R; ++j) {
+                const int p = warp * 32 * R + j * 32 + lane;
+                const uint32_t key = ks[p];
+                const uint32_t d = (key >> shift) & 255u;
+                const uint32_t pos = cnt[d * kCntStride + warp] + rankS[p];
+                kd[pos] = key;
+                id[pos] = pass == 0 ? static_cast<uint16_t>(p) : is[p];
+            }
+            __syncthreads();
+        }
+        // after four passes the sorted keys and indices are in keyA / idxA
+
+        if (gapOut) {
+            uint32_t* gnat = cnt;
+            for (int k0 = warp * 32; k0 < gapWords * 32; k0 += kSortThreads) {
+                const int k = k0 + lane;
+                const float v0 = k < n ? __uint_as_float(radix_key_inv(keyA[k])) : 0.0f;
+                float v1 = __shfl_down_sync(0xffffffffu, v0, 1);
+                if (lane == 31 && k + 1 < n) v1 = __uint_as_float(radix_key_inv(keyA[k + 1]));
+                const uint32_t bits = __ballot_sync(0xffffffffu, k + 1 < n && __fadd_rn(v0, 1e-7f) < v1);
+                if (lane == 0) gnat[k0 >> 5] = bits;
+            }
+            __syncthreads();
+            uint16_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
+            for (int j = tid; j < 2 * L; j += kSortThreads) {
+                const int k = (j & 31) * L + 16 * (j >> 5);
+                grow[j] = k < n ? static_cast<uint16_t>(gnat[k >> 5] >> (k & 31)) : uint16_t(0);
+            }
+        }
+        uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
+        if (ordPadded) {
+            // lane-run layout; positions from n to the next multiple of 8 hold
+            // the zero slot (one weight copy: slot n)
+            const int n8 = (n + 7) & ~7;
+            const uint32_t zs = static_cast<uint32_t>(zero_slot(n, 0));
+            for (int k = tid * 8; k < n8; k += kSortThreads * 8) {
+                uint4 v = *reinterpret_cast<const uint4*>(idxA + k);
+                if (k + 8 > n) {
+                    uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        if (k + e >= n) w4[e >> 1] = (w4[e >> 1] & ~(0xFFFFu << (16 * (e & 1)))) | (zs << (16 * (e & 1)));
+                    v = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                }
+                *reinterpret_cast<uint4*>(orow + ord_slot(k, L)) = v;
+            }
+        } else {
+            for (int k = tid; k < n; k += kSortThreads) orow[k] = idxA[k];
         }
         __syncthreads();
     }
@@ -767,7 +919,10 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
 }
 
 // 5. Winner -> TileBestCandidate with theta = 0.5f * (v[k] + v[k+1]).
-__global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const uint32_t* __restrict__ sumT,
+// feats and the candidate indices are relative to the searched range, which
+// starts at featBase of the pool; the output featureIdx is the pool's.
+__global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, int featBase,
+                                const uint32_t* __restrict__ sumT,
                                 const float* __restrict__ invNorm, int n, const uint16_t* __restrict__ ord,
                                 int64_t ordStride, int slotBase, int L, RoundParams* __restrict__ prm,
                                 const int8_t* __restrict__ refParity, const int* __restrict__ refSplit,
@@ -793,10 +948,38 @@ __global__ void finalize_kernel(const vj_haar_feature* __restrict__ feats, const
         const float v1 = train_response(ft, sumT, n, s1, invNorm[s1]);
         b.bestErr = __uint_as_float(static_cast<uint32_t>(w >> 32));
         b.bestTheta = __fmul_rn(0.5f, __fadd_rn(v0, v1));
-        b.featureIdx = f;
+        b.featureIdx = featBase + f;
         b.bestParity = refParity[f];
     }
     *out = b;
+}
+
+// ReduceTileBestCandidatesKernel (main.cu:991-1028): the best of n tile (or
+// rank) candidates, lower FP32 error first, then lower featureIdx; one warp.
+__device__ __forceinline__ vj_tile_best better_tile(const vj_tile_best& a, const vj_tile_best& b) {
+    if (b.bestErr < a.bestErr) return b;
+    if (b.bestErr > a.bestErr) return a;
+    return b.featureIdx < a.featureIdx ? b : a;
+}
+
+__global__ void reduce_tile_best_kernel(const vj_tile_best* __restrict__ in, int n, vj_tile_best* __restrict__ out) {
+    vj_tile_best best;
+    best.bestErr = INFINITY;
+    best.bestTheta = 0.0f;
+    best.featureIdx = INT_MAX;
+    best.bestParity = 1;
+    best.pad0 = best.pad1 = best.pad2 = 0;
+    for (int i = threadIdx.x; i < n; i += 32) best = better_tile(best, in[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        vj_tile_best other = best;
+        other.bestErr = __shfl_xor_sync(0xffffffffu, best.bestErr, o);
+        other.bestTheta = __shfl_xor_sync(0xffffffffu, best.bestTheta, o);
+        other.featureIdx = __shfl_xor_sync(0xffffffffu, best.featureIdx, o);
+        other.bestParity = static_cast<int8_t>(__shfl_xor_sync(0xffffffffu, static_cast<int>(best.bestParity), o));
+        best = better_tile(best, other);
+    }
+    if (threadIdx.x == 0) *out = best;
 }
 
 // ---------------------------------------------------------------------------
@@ -1175,9 +1358,12 @@ int sm_count() {
 int refine_blocks() { return sm_count(); }
 
 // Launches eval_sort_kernel with the smallest items-per-thread that holds n.
+// keyScratch / idxScratch: 2 * 1024 * large_sort_r(n) keys and indices per
+// CTA of the launch (min(featCount, SMs) CTAs), used only for n > 32768.
 int launch_eval_sort(const vj_haar_feature* feats, int featBegin, int featCount, const uint32_t* sumT,
                      const float* invNorm, int n, const float* resp, uint16_t* ordOut, int64_t ordStride,
-                     bool ordPadded, uint16_t* gapOut, int64_t gapStride, int slotBase, int L, cudaStream_t stream) {
+                     bool ordPadded, uint16_t* gapOut, int64_t gapStride, int slotBase, int L, uint32_t* keyScratch,
+                     uint16_t* idxScratch, cudaStream_t stream) {
     const int grid = std::min(featCount, sm_count());
     auto go = [&](auto kernel, size_t smem) -> int {
         VJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
@@ -1199,7 +1385,18 @@ int launch_eval_sort(const vj_haar_feature* feats, int featBegin, int featCount,
     VJ_SORT_CASE(24)
     VJ_SORT_CASE(32)
 #undef VJ_SORT_CASE
-    return set_error(VJ_INVALID_ARG, "on-chip sort holds at most 32768 samples per feature");
+    const int R = large_sort_r(n);
+    if (R > kLargeSortMaxR) return set_error(VJ_INVALID_ARG, "the sort holds at most 65535 samples per feature");
+    if (!keyScratch || !idxScratch) return set_error(VJ_RUNTIME_ERROR, "sort: no scratch for more than 32768 samples");
+    auto kernel = resp ? eval_sort_large_kernel<true> : eval_sort_large_kernel<false>;
+    const size_t smem = large_sort_smem_bytes(R);
+    VJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    VJ_TIMED_LAUNCH("eval_sort_kernel", stream,
+                    kernel<<<grid, kSortThreads, smem, stream>>>(feats, featBegin, featCount, sumT, invNorm, n, resp,
+                                                                 ordOut, ordStride, ordPadded, gapOut, gapStride, L, R,
+                                                                 keyScratch, idxScratch));
+    VJ_LAUNCH_CHECK("eval_sort_large_kernel");
+    return VJ_OK;
 }
 
 }  // namespace
@@ -1211,6 +1408,9 @@ struct vj_trainer {
     int winW = 24, winH = 24, maxSamples = 0;
     vj_haar_feature* d_feat = nullptr;
     int64_t nFeat = 0;
+    // Features searched by vj_stump_search: [rangeBegin, rangeBegin + rangeCount)
+    // of the pool (rangeCount < 0: the whole pool).
+    int64_t rangeBegin = 0, rangeCount = -1;
     const uint32_t* d_sumT = nullptr;
     const float* d_invNorm = nullptr;
     int n = 0;
@@ -1225,6 +1425,10 @@ struct vj_trainer {
     int slotBase = 0;  // > 0: resident orders hold two-copy shared-memory slots
     int laneRun = 16;  // L of the resident layout (lane_run(n))
     bool prepared = false;
+    // Keys and indices of the sort above 32,768 samples (per CTA of the launch).
+    uint32_t* d_sortKeys = nullptr;
+    uint16_t* d_sortIdx = nullptr;
+    size_t sortScratchPositions = 0;
     // Per-round scratch.
     float* d_wsg = nullptr;
     float* d_fastErr = nullptr;
@@ -1283,6 +1487,26 @@ int ensure_round_scratch(vj_trainer* t) {
     return VJ_OK;
 }
 
+// The global scratch of the sort for n > 32768: two key and two index
+// buffers of 1024 * large_sort_r(n) positions for each CTA (one per SM).
+int ensure_sort_scratch(vj_trainer* t, int n) {
+    if (n <= kOnChipSortMax) return VJ_OK;
+    const size_t positions = static_cast<size_t>(sm_count()) * 2 * 1024 * large_sort_r(n);
+    if (positions <= t->sortScratchPositions) return VJ_OK;
+    cudaFree(t->d_sortKeys);
+    cudaFree(t->d_sortIdx);
+    t->d_sortKeys = nullptr;
+    t->d_sortIdx = nullptr;
+    t->sortScratchPositions = 0;
+    VJ_CUDA_TRY(cudaMalloc(&t->d_sortKeys, positions * sizeof(uint32_t)));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_sortIdx, positions * sizeof(uint16_t)));
+    t->sortScratchPositions = positions;
+    return VJ_OK;
+}
+
+int64_t range_begin(const vj_trainer* t) { return t->rangeCount < 0 ? 0 : t->rangeBegin; }
+int64_t range_count(const vj_trainer* t) { return t->rangeCount < 0 ? t->nFeat : t->rangeCount; }
+
 int check_bound(vj_trainer* t, const char* fn) {
     if (!t) return set_error(VJ_INVALID_ARG, std::string(fn) + ": null trainer");
     if (!t->d_feat || t->nFeat <= 0) return set_error(VJ_INVALID_ARG, std::string(fn) + ": no feature pool set");
@@ -1295,8 +1519,9 @@ int sort_all(vj_trainer* t, cudaStream_t s) {
     const int L = lane_run(t->n);
     const int64_t ordStride = 32 * static_cast<int64_t>(L);  // 32 lane runs
     const int64_t gapStride = 2 * static_cast<int64_t>(L);   // 16-bit words
-    const size_t ordBytes = static_cast<size_t>(t->nFeat) * ordStride * sizeof(uint16_t);
-    const size_t gapBytes = static_cast<size_t>(t->nFeat) * gapStride * sizeof(uint16_t);
+    const int64_t F = range_count(t);
+    const size_t ordBytes = static_cast<size_t>(F) * ordStride * sizeof(uint16_t);
+    const size_t gapBytes = static_cast<size_t>(F) * gapStride * sizeof(uint16_t);
     if (ordBytes > t->ordBytes) {
         cudaFree(t->d_ord);
         t->d_ord = nullptr;
@@ -1315,8 +1540,12 @@ int sort_all(vj_trainer* t, cudaStream_t s) {
     t->gapStride = gapStride;
     t->slotBase = t->n <= kTwoCopyMax ? two_copy_base(t->n) : 0;
     t->laneRun = L;
-    return launch_eval_sort(t->d_feat, 0, static_cast<int>(t->nFeat), t->d_sumT, t->d_invNorm, t->n, nullptr,
-                            t->d_ord, ordStride, true, t->d_gap, gapStride, t->slotBase, L, s);
+    const int st = ensure_sort_scratch(t, t->n);
+    if (st != VJ_OK) return st;
+    return launch_eval_sort(t->d_feat, static_cast<int>(range_begin(t)), static_cast<int>(F), t->d_sumT,
+                            t->d_invNorm, t->n, nullptr,
+                            t->d_ord, ordStride, true, t->d_gap, gapStride, t->slotBase, L, t->d_sortKeys,
+                            t->d_sortIdx, s);
 }
 
 }  // namespace
@@ -1354,6 +1583,8 @@ int vj_trainer_destroy(vj_trainer* t) {
     cudaFree(t->d_refSplit);
     cudaFree(t->d_prm);
     cudaFree(t->d_status);
+    cudaFree(t->d_sortKeys);
+    cudaFree(t->d_sortIdx);
     delete t;
     return ok();
 }
@@ -1380,6 +1611,8 @@ int vj_trainer_set_features(vj_trainer* t, const vj_haar_feature* features, int6
     cudaFree(t->d_feat);
     t->d_feat = nullptr;
     t->nFeat = 0;
+    t->rangeBegin = 0;
+    t->rangeCount = -1;
     t->prepared = false;
     VJ_CUDA_TRY(cudaMalloc(&t->d_feat, sizeof(vj_haar_feature) * count));
     VJ_CUDA_TRY(cudaMemcpy(t->d_feat, features, sizeof(vj_haar_feature) * count, cudaMemcpyHostToDevice));
@@ -1426,7 +1659,7 @@ int vj_trainer_last_round(vj_trainer* t, vj_round_info* out) {
         for (int k = 0; k < std::min(nc, 2); ++k) {
             if (keys[static_cast<size_t>(k)] == ~0ull) break;
             const float e = bits_float(static_cast<int32_t>(keys[static_cast<size_t>(k)] >> 32));
-            const int f = static_cast<int>(keys[static_cast<size_t>(k)] & 0xFFFFFFFFull);
+            const int f = static_cast<int>(keys[static_cast<size_t>(k)] & 0xFFFFFFFFull) + static_cast<int>(range_begin(t));
             if (k == 0) {
                 out->bestErr = e;
                 out->bestFeature = f;
@@ -1441,7 +1674,7 @@ int vj_trainer_last_round(vj_trainer* t, vj_round_info* out) {
 
 int vj_trainer_stage_bytes(vj_trainer* t, int n, int64_t* bytes) {
     if (!t || !bytes || n <= 0) return set_error(VJ_INVALID_ARG, "vj_trainer_stage_bytes: bad arguments");
-    *bytes = t->nFeat * (static_cast<int64_t>(lane_run(n)) * (32 * 2 + 2 * 2));
+    *bytes = range_count(t) * (static_cast<int64_t>(lane_run(n)) * (32 * 2 + 2 * 2));
     return ok();
 }
 
@@ -1451,6 +1684,24 @@ int vj_trainer_prepare_stage(vj_trainer* t, void* stream) {
     st = sort_all(t, static_cast<cudaStream_t>(stream));
     if (st != VJ_OK) return st;
     t->prepared = true;
+    return ok();
+}
+
+int vj_trainer_set_search_range(vj_trainer* t, int64_t featureBegin, int64_t featureCount) {
+    if (!t || !t->d_feat) return set_error(VJ_INVALID_ARG, "vj_trainer_set_search_range: no feature pool set");
+    if (featureBegin < 0 || featureCount <= 0 || featureBegin + featureCount > t->nFeat)
+        return set_error(VJ_INVALID_ARG, "vj_trainer_set_search_range: range outside the feature pool");
+    t->rangeBegin = featureBegin;
+    t->rangeCount = featureCount;
+    t->prepared = false;
+    return ok();
+}
+
+int vj_reduce_tile_best(const vj_tile_best* d_in, int count, vj_tile_best* d_out, void* stream) {
+    if (!d_in || !d_out || count <= 0) return set_error(VJ_INVALID_ARG, "vj_reduce_tile_best: bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VJ_TIMED_LAUNCH("reduce_tile_best_kernel", s, reduce_tile_best_kernel<<<1, 32, 0, s>>>(d_in, count, d_out));
+    VJ_LAUNCH_CHECK("reduce_tile_best_kernel");
     return ok();
 }
 
@@ -1471,7 +1722,9 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
     }
     st = ensure_round_scratch(t);
     if (st != VJ_OK) return st;
-    const int F = static_cast<int>(t->nFeat), n = t->n;
+    const int F = static_cast<int>(range_count(t)), n = t->n;
+    const int fb = static_cast<int>(range_begin(t));
+    const uint8_t* usedRange = d_usedMask ? d_usedMask + fb : nullptr;
     VJ_TIMED_LAUNCH("prep_round_kernel", s,
                     prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, n, t->d_wsg, t->d_prm,
                                                          t->d_gate));
@@ -1489,7 +1742,7 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("sweep_kernel", s,
                         k<<<grid, tpb, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb,
-                                                    t->laneRun, F, d_usedMask, t->d_prm, t->d_fastErr, t->d_gate));
+                                                    t->laneRun, F, usedRange, t->d_prm, t->d_fastErr, t->d_gate));
         VJ_LAUNCH_CHECK("sweep_kernel");
     }
     VJ_TIMED_LAUNCH("select_candidates_kernel", s,
@@ -1508,7 +1761,8 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_LAUNCH_CHECK("refine_kernel");
     }
     VJ_TIMED_LAUNCH("finalize_kernel", s,
-                    finalize_kernel<<<1, 32, 0, s>>>(t->d_feat, t->d_sumT, t->d_invNorm, n, t->d_ord, t->ordStride,
+                    finalize_kernel<<<1, 32, 0, s>>>(t->d_feat + fb, fb, t->d_sumT, t->d_invNorm, n, t->d_ord,
+                                                     t->ordStride,
                                                      sb, t->laneRun, t->d_prm, t->d_refParity, t->d_refSplit, d_out,
                                                      t->d_gate));
     VJ_LAUNCH_CHECK("finalize_kernel");
@@ -1568,8 +1822,10 @@ int vj_trainer_sort_per_feature(vj_trainer* t, const float* d_resp, int featureC
                                 void* stream) {
     if (!t || !d_resp || !d_sortedIdx || featureCount <= 0 || t->n <= 0)
         return set_error(VJ_INVALID_ARG, "vj_trainer_sort_per_feature: bad arguments");
-    const int st = launch_eval_sort(nullptr, 0, featureCount, nullptr, nullptr, t->n, d_resp, d_sortedIdx, t->n,
-                                    false, nullptr, 0, 0, 16, static_cast<cudaStream_t>(stream));
+    int st = ensure_sort_scratch(t, t->n);
+    if (st != VJ_OK) return st;
+    st = launch_eval_sort(nullptr, 0, featureCount, nullptr, nullptr, t->n, d_resp, d_sortedIdx, t->n, false, nullptr,
+                          0, 0, 16, t->d_sortKeys, t->d_sortIdx, static_cast<cudaStream_t>(stream));
     return st == VJ_OK ? ok() : st;
 }
 

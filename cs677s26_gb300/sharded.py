@@ -1,22 +1,25 @@
 """Feature-range sharding of the best-weak search over ranks (one GPU each).
 
 The stump search is independent per feature, so ranks split the pool into
-contiguous feature ranges.  Each rank finds its range's best stump with the
-reference's exact pick rule (vj_stump_search with the features outside its
-range marked used, or a trainer over its range), and one exchange per round -
-an all-gather of one (FP32 error, featureIdx, theta, parity) record per rank -
-selects the global pick by the reference's cross-feature rule: lower FP32
-error, then lower featureIdx (ReduceTileBestCandidatesKernel and
-SelectBestInTileKernel's tie-break, src/main.cu:999-1028,
-src/boosting_core.cu:87-99).  Every rank then applies the same round update,
-so weights stay identical across ranks without further traffic.
+contiguous feature ranges, the reference's feature tiles
+(src/main.cu:2013-2053).  Each rank sorts and searches only its range
+(AdaBoostTrainer.setSearchRange: its resident orders and sweeps cover that
+range alone) and finds the range's best stump with the reference's exact pick
+rule.  One exchange per round - an all-gather of one 16-byte candidate
+(vj_tile_best) per rank into a device array, reduced on the device by
+vj_reduce_tile_best, the reference's ReduceTileBestCandidatesKernel
+(src/main.cu:991-1028: lower FP32 error, then lower featureIdx) - gives every
+rank the global pick, and every rank applies the same round update, so the
+weights stay identical across ranks without further traffic.
 
 This is the only collective of the training path; detection and serving
 shard by image with no collective at all.
+
+Host-side helpers (pick_global, exchange_best) apply the same rule to plain
+records, for ranks that search with the CPU oracle.
 """
 from __future__ import annotations
 
-import struct
 from typing import Sequence
 
 import numpy as np
@@ -32,15 +35,14 @@ def feature_range(n_features: int, rank: int, world: int) -> tuple[int, int]:
     return n_features * rank // world, n_features * (rank + 1) // world
 
 
-def _key(rec) -> tuple[int, int]:
-    """Order of the reference's cross-feature rule: FP32 error (as an ordered
-    integer; NaN/inf never win), then featureIdx."""
+def _key(rec) -> tuple[float, int]:
+    """The reference's cross-candidate order: FP32 error compared as a float
+    (so -0.0 and +0.0 tie), then featureIdx; records without a valid split
+    (featureIdx < 0, or an infinite or NaN error) come last."""
     e = float(np.float32(rec["err"]))
     if not np.isfinite(e) or rec["featureIdx"] < 0:
-        return (2**32, 2**31)
-    bits = struct.unpack("<I", struct.pack("<f", e))[0]
-    ordered = bits ^ 0x80000000 if bits < 0x80000000 else ~bits & 0xFFFFFFFF  # float order as unsigned
-    return (ordered, int(rec["featureIdx"]))
+        return (float("inf"), 2**31)
+    return (e, int(rec["featureIdx"]))
 
 
 def pick_global(records: Sequence) -> np.void:
@@ -50,8 +52,8 @@ def pick_global(records: Sequence) -> np.void:
 
 
 def exchange_best(local, group=None) -> np.void:
-    """All-gathers every rank's local pick (torch.distributed, any backend)
-    and returns the global one; `local` has the RECORD fields, featureIdx
+    """All-gathers every rank's local pick on the host (any backend) and
+    returns the global one; `local` has the RECORD fields, featureIdx
     already global."""
     import torch
     import torch.distributed as dist
@@ -60,18 +62,43 @@ def exchange_best(local, group=None) -> np.void:
     for k in RECORD.names:
         rec[k] = local[k]
     words = torch.from_numpy(rec.view(np.int32).copy())
-    if dist.get_backend(group) == "nccl":
-        words = words.cuda()
     world = dist.get_world_size(group)
     out = [torch.zeros_like(words) for _ in range(world)]
     dist.all_gather(out, words, group=group)
-    allrec = np.concatenate([o.cpu().numpy() for o in out]).view(RECORD)
+    allrec = np.concatenate([o.numpy() for o in out]).view(RECORD)
     return pick_global(allrec)
 
 
+def exchange_best_device(local, out, gathered=None, group=None, stream=None):
+    """The round's exchange on the device.  `local` is this rank's candidate
+    (a CUDA int32 tensor of 4 words: vj_tile_best) and `out` receives the
+    global pick (same shape).  With NCCL the candidates are all-gathered into
+    a device array with no host synchronisation; other backends (gloo) move
+    the 16 bytes through the host.  The array is then reduced on the device by
+    vj_reduce_tile_best.  `gathered` may hold a reusable int32 CUDA buffer of
+    4 * world words."""
+    import torch
+    import torch.distributed as dist
+
+    from . import _capi
+
+    world = dist.get_world_size(group)
+    if gathered is None:
+        gathered = torch.empty(4 * world, dtype=torch.int32, device=local.device)
+    if dist.get_backend(group) == "nccl":
+        dist.all_gather_into_tensor(gathered, local, group=group)
+    else:
+        parts = [torch.zeros(4, dtype=torch.int32) for _ in range(world)]
+        dist.all_gather(parts, local.cpu(), group=group)
+        gathered.copy_(torch.cat(parts))
+    _capi.call("vj_reduce_tile_best", gathered.data_ptr(), world, out.data_ptr(),
+               None if stream is None else int(stream))
+    return out
+
+
 def range_used_mask(n_features: int, rank: int, world: int) -> np.ndarray:
-    """A used-feature mask that keeps a full-pool trainer to this rank's range
-    (vj_stump_search skips features marked used)."""
+    """A used-feature mask that keeps a full-pool search to this rank's range
+    (features marked used are skipped), for ranks searching with the oracle."""
     b, e = feature_range(n_features, rank, world)
     m = np.ones(n_features, np.uint8)
     m[b:e] = 0

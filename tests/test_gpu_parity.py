@@ -147,6 +147,57 @@ def test_weak_search_both_weight_layouts(cuda, vj, oracle, basic_pool, n):
         used[got[0]] = 1
 
 
+@pytest.mark.parametrize("n,with_active", [(32769, False), (40000, False), (65535, False), (40000, True)])
+def test_weak_search_beyond_on_chip_sort(cuda, vj, oracle, basic_pool, n, with_active):
+    """From 32,769 samples up to the reference's limit of 65,535 (16-bit sample
+    indices, boosting_core.cu:704 and :851) the sort keeps its keys and
+    indices in a global scratch and the sweep reads one weight copy (from
+    shared memory up to 49,152 samples, from global memory above).  The first
+    round re-sorts inside the search, the next two use the resident orders;
+    every round gives the oracle's pick."""
+    npos = n // 2
+    p = vj.synth_patches(61, npos, n - npos)
+    labels = np.array([1] * npos + [-1] * (n - npos), np.int8)
+    feats = np.ascontiguousarray(basic_pool[::317][:512])
+    rng = np.random.default_rng(n)
+    w = (rng.random(n) / n).astype(np.float32)
+    active = (rng.random(n) > 0.2).astype(np.uint8) if with_active else None
+    T = Train(cuda, vj, oracle, p, labels, feats, w, active)
+    sums, inv = oracle.train_integrals(p)
+    used = np.zeros(len(feats), np.uint8)
+    weak = cuda.zeros(7, dtype=cuda.int32, device="cuda")
+    for r in range(3):
+        if r == 1:
+            assert T.t.prepareStage() == 0
+        got = T.search(used=True)
+        ref = oracle.weak_search(feats, sums, inv, labels, T.w.cpu().numpy(), active=active, used=used, threads=16)
+        assert got == (ref["featureIdx"], ref["err"], ref["theta"], ref["parity"]), r
+        assert T.t.applyBestWeak(T.best, T.strong, T.used, weak) == 0
+        used[got[0]] = 1
+
+
+def test_step_api_sort_beyond_on_chip_sort(cuda, vj, oracle, basic_pool):
+    """sortSamplesPerFeature at 40,001 samples: the stable order of the radix
+    keys, -0.0 before +0.0 (a flat patch has invNorm 0)."""
+    torch = cuda
+    n, F = 40001, 40
+    p = vj.synth_patches(63, 20000, n - 20000)
+    p[11] = 77  # flat: responses +-0.0
+    labels = np.array([1] * 20000 + [-1] * (n - 20000), np.int8)
+    feats = np.ascontiguousarray(basic_pool[::4001][:F])
+    T = Train(cuda, vj, oracle, p, labels, feats, np.full(n, np.float32(1.0 / n), np.float32))
+    resp = torch.empty(F * n, dtype=torch.float32, device="cuda")
+    assert T.t.evaluateFeatureResponses(0, F, resp) == 0
+    order = torch.empty(F * n, dtype=torch.int16, device="cuda")
+    assert T.t.sortSamplesPerFeature(resp, F, order) == 0
+    R = resp.cpu().numpy().reshape(F, n)
+    O_ = order.cpu().numpy().view(np.uint16).reshape(F, n)
+    bits = R.view(np.uint32)
+    keys = np.where(bits >> 31, ~bits, bits | np.uint32(0x80000000))
+    for f in range(F):
+        assert np.array_equal(O_[f], np.lexsort((np.arange(n), keys[f]))), f
+
+
 @pytest.mark.parametrize("n", [2, 3, 17, 33, 100, 511, 513, 1000])
 def test_weak_search_small_and_ragged_counts(cuda, vj, oracle, basic_pool, n):
     """Sample counts around the sweep's 16-position lane runs, its 512-position

@@ -80,9 +80,13 @@ def test_pick_global_rule():
     recs = [(0.25, 90, 1.0, 1), (0.125, 500, 2.0, -1), (0.125, 40, 3.0, 1), (float("inf"), 1, 0.0, 1),
             (-0.0, 600, 0.0, 1), (0.0, 700, 0.0, 1)]
     g = sharded.pick_global(recs)
-    assert g["featureIdx"] == 600  # -0.0 orders before +0.0 and every positive error
+    assert g["featureIdx"] == 600  # below every positive error; -0.0 and +0.0 tie, the lower index wins
+    g = sharded.pick_global([(0.0, 600, 0.0, 1), (-0.0, 700, 0.0, 1)])
+    assert g["featureIdx"] == 600  # as in the reference's float comparison, not the sign bit
     g = sharded.pick_global(recs[:4])
     assert g["featureIdx"] == 40 and g["theta"] == np.float32(3.0)
+    g = sharded.pick_global([(float("inf"), -1, 0.0, 1), (float("inf"), -1, 0.0, 1)])
+    assert g["featureIdx"] == -1  # no rank has a valid split
 
 
 def test_two_ranks_equal_single_process():
