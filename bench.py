@@ -703,7 +703,7 @@ def run_reference(args, rank, world):
     sums, inv = O.train_integrals(patches)
     threads = os.cpu_count() or 1
     n = len(patches)
-    stride = max(1, len(pool) // (32 * threads))
+    stride = max(1, len(pool) // (128 * threads))
     for _ in range(args.warmup):
         cpu_sample(O, pool, sums, inv, stride * 4, threads)
     runs = [cpu_sample(O, pool, sums, inv, stride, threads) for _ in range(args.steps)]
