@@ -54,12 +54,13 @@ SERVER_STATS = np.dtype([("submitted", "<i8"), ("completed", "<i8"), ("failed", 
                          ("peakAdmittedBytes", "<i8"), ("deviceBytes", "<i8")])
 ROUND_INFO = np.dtype([("fastMin", "<f4"), ("window", "<f4"), ("candidates", "<i4"), ("status", "<i4"),
                        ("totalPos", "<f4"), ("totalNeg", "<f4"), ("bestErr", "<f4"), ("bestFeature", "<i4"),
-                       ("runnerUpErr", "<f4"), ("runnerUpFeature", "<i4")])
+                       ("runnerUpErr", "<f4"), ("runnerUpFeature", "<i4"), ("swept", "<i4"), ("pad0", "<i4"),
+                       ("sweptTotal", "<i8")])
 PHASES = ("pyramid", "integrals", "tile_pass", "queue_passes", "deep_pass", "grouping", "output")
 HOST_PHASES = ("plan_upload", "wait", "post")
 
 assert DETECT_STATS.itemsize == 160 and DETECT_CONFIG.itemsize == 24
-assert SERVER_CONFIG.itemsize == 72 and SERVER_STATS.itemsize == 112 and ROUND_INFO.itemsize == 40
+assert SERVER_CONFIG.itemsize == 72 and SERVER_STATS.itemsize == 112 and ROUND_INFO.itemsize == 56
 assert HAAR_FEATURE.itemsize == 64 and STUMP4.itemsize == 16 and STAGE.itemsize == 12
 assert DETECTION.itemsize == 24 and TILE_BEST.itemsize == 16 and WEAK.itemsize == 28
 

@@ -18,7 +18,7 @@ static_assert(sizeof(vj_tile_best) == 16, "TileBestCandidate layout");
 static_assert(sizeof(vj_feature_best_split) == 16, "FeatureBestSplit layout");
 static_assert(sizeof(vj_weak_classifier) == 28, "WeakClassifier layout");
 static_assert(sizeof(vj_detect_stats) == 160 && sizeof(vj_detect_config) == 24, "detection record layouts");
-static_assert(sizeof(vj_round_info) == 40, "round statistics layout");
+static_assert(sizeof(vj_round_info) == 56, "round statistics layout");
 static_assert(sizeof(vj_server_config) == 72 && sizeof(vj_server_stats) == 112, "server record layouts");
 
 // Records a message for vj_last_error() and returns `status`.

@@ -49,7 +49,6 @@ namespace {
 constexpr int kSortThreads = 1024;
 constexpr int kCntStride = 33;  // per-digit row of 32 warp counters, padded against bank conflicts
 constexpr int kSweepThreads = 512;
-constexpr int kSweepWarps = kSweepThreads / 32;
 constexpr int kSmemWeightsMax = 49152;  // samples whose weights fit in shared memory
 constexpr int kRefineThreads = 256;
 constexpr int kRefineWarps = kRefineThreads / 32;
@@ -149,6 +148,24 @@ struct RoundParams {
     unsigned long long winner;   // (FP32 error bits << 32) | featureIdx; min wins
     int np, nn;                  // active positive / negative sample counts
     int status;                  // 0 ok, 1 no valid split anywhere
+    float bfast;                 // bound of |fast error - exact error| (rounded up)
+    float lbScale;               // factor taking last round's bounds to this round's weights
+    int pruneOK;                 // 1: the bounds hold for this round's weights
+    unsigned int nextFeat;       // feature counter of the sweep's work distribution
+    int swept;                   // features the sweep streamed this round
+};
+
+// Bounds that let the sweep skip features (see sweep_kernel).  Within a
+// stage, one AdaBoost update multiplies every active weight by 1 or F and
+// divides it by Z, so a feature's exact best error after the update is at
+// least min(1, F) / Z times its error before; `scale` is that factor of the
+// last update (rounded down, with room for the FP32 rounding of the new
+// weights), and `valid` says whether the per-feature bounds and the weight
+// shadow describe the current weights.
+struct PruneState {
+    double F;      // exp(C) of the last update
+    float scale;   // min(1, F) / Z * (1 - 4u), at most 1
+    int valid;
 };
 
 // Mask of the lanes of the warp whose 8-bit digit equals this lane's, from 8
@@ -537,18 +554,36 @@ eval_sort_large_kernel(const vj_haar_feature* __restrict__ feats, int featBegin,
 // Per-round weight preparation: signed weights (+w positive, -w negative,
 // +-0 inactive), totals and the candidate window.
 // ---------------------------------------------------------------------------
+// With wShadow / aShadow given (the resident search), the kernel also decides
+// whether last round's per-feature bounds may prune this round's sweep: only
+// when the weights are bit for bit what the last vj_round_update left
+// (wShadow) and the active mask is what the last search saw (aShadow), i.e.
+// nothing but that update changed them.
 __global__ void __launch_bounds__(1024)
 prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
                   const float* __restrict__ weight, int n, float* __restrict__ wsg,
-                  RoundParams* __restrict__ prm, const int* gate) {
+                  RoundParams* __restrict__ prm, const float* __restrict__ wShadow, uint8_t* __restrict__ aShadow,
+                  const PruneState* __restrict__ ps, const int* gate) {
     if (gate_closed(gate)) return;
     __shared__ double sp[32], sn[32];
     __shared__ int cp[32], cn[32];
+    __shared__ int changed;
     double tp = 0.0, tn = 0.0;
     int np = 0, nn = 0;
-    if (threadIdx.x == 0) wsg[n] = 0.0f;  // the zero slot of one-copy orders
+    if (threadIdx.x == 0) {
+        wsg[n] = 0.0f;  // the zero slot of one-copy orders
+        changed = 0;
+    }
+    __syncthreads();
+    int diff = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const bool act = active == nullptr || active[i] != 0;
+        if (wShadow) {
+            diff |= __float_as_uint(weight[i]) != __float_as_uint(wShadow[i]);
+            const uint8_t a = act ? 1 : 0;
+            diff |= aShadow[i] != a;
+            aShadow[i] = a;
+        }
         const float w = act ? weight[i] : 0.0f;
         const bool pos = label[i] > 0;
         wsg[i] = pos ? w : -w;
@@ -575,6 +610,7 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
         cp[warp] = np;
         cn[warp] = nn;
     }
+    if (diff) changed = 1;
     __syncthreads();
     if (threadIdx.x == 0) {
         double TP = 0.0, TN = 0.0;
@@ -607,6 +643,11 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
         prm->np = NP;
         prm->nn = NN;
         prm->status = 0;
+        prm->bfast = __double2float_ru(bfast);
+        prm->pruneOK = (wShadow && ps->valid && !changed) ? 1 : 0;
+        prm->lbScale = prm->pruneOK ? ps->scale : 0.0f;
+        prm->nextFeat = 0;
+        prm->swept = 0;
     }
 }
 
@@ -614,13 +655,15 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
 // 2. Fast sweep: one warp per feature, minimum weighted error to within the
 //    bound used for the window.
 // ---------------------------------------------------------------------------
+constexpr int kSweepChunk = 4;  // features a warp takes from the shared counter at once
+
 template <bool kSmemW, int TPB>
 __global__ void __launch_bounds__(TPB, 1024 / TPB)
 sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t* __restrict__ gap,
              int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, int L, int featCount,
              const uint8_t* __restrict__ usedMask, RoundParams* __restrict__ prm,
-             float* __restrict__ fastErr, const int* gate) {
-    constexpr int kSweepWarps = TPB / 32;
+             float* __restrict__ fastErr, float* __restrict__ lb, unsigned long long* __restrict__ sweptTotal,
+             const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ float wsgS[];
     const float* wsg = wsgG;
@@ -640,49 +683,104 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
     // feature's end one warp scan gives each lane the sum of the runs before
     // its own, which is added once.  Rounding is monotone, so
     // min_i fl(b + s_i) = fl(b + min_i s_i).  Padding positions carry the zero
-    // slot and no split bit, so no position needs a mask.  Each warp walks the
-    // flattened sequence of (feature, step) items of the features it owns; the
-    // loads of the next item are issued before the current one is processed,
-    // across feature boundaries.
+    // slot and no split bit, so no position needs a mask.  A warp walks the
+    // (feature, step) items of the features it takes; the loads of the next
+    // item are issued before the current one is processed, across feature
+    // boundaries.
+    //
+    // Features come in chunks of kSweepChunk from a counter shared by all
+    // warps.  When a warp reaches a feature it compares the feature's bound -
+    // a lower bound of its exact best error under this round's weights: last
+    // round's fast error minus the fast pass's error bound, or last round's
+    // bound, times the update's factor lbScale - with the round's running
+    // minimum of the fast errors.  A feature whose bound exceeds that minimum
+    // plus the candidate window has exact error above (minimum exact error)
+    // + 2 x (the reference's FP32 error bound), so it cannot be the
+    // reference's pick and is not streamed: its fast error is +inf (no
+    // candidate) and its bound is kept for the next round.  Streamed features
+    // leave fresh bounds.
     const float TP = prm->tp, TN = prm->tn;
+    const float window = prm->window, bfast = prm->bfast, scale = prm->lbScale;
+    const bool prune = prm->pruneOK != 0;
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
-    const int nw = gridDim.x * kSweepWarps;
     const int spf = L >> 4;  // steps per feature
-    const int myFeat = gw < featCount ? (featCount - gw + nw - 1) / nw : 0;
-    const int items = myFeat * spf;
     const uint32_t z = static_cast<uint32_t>(zero_slot(n, slotBase)) * 0x10001u;
-    // Used features are streamed like the others and dropped at the end, so
-    // no load waits on the mask.
-    auto load = [&](int it, int f, int t, uint4& a, uint4& b, uint32_t& g) {
+    const volatile unsigned int* runMinBits = &prm->fastMinBits;
+    float runMin = INFINITY;  // the warp's view of the running minimum (warp-uniform)
+    int qBase = 0;
+    unsigned qMask = 0;  // features of the warp's chunk not yet reached
+    int swept = 0;
+    // The next feature to stream (warp-uniform), or -1 when none is left.
+    auto next_feature = [&]() -> int {
+        for (;;) {
+            if (qMask == 0) {
+                int c0 = 0;
+                if (lane == 0) c0 = static_cast<int>(atomicAdd(&prm->nextFeat, static_cast<unsigned>(kSweepChunk)));
+                c0 = __shfl_sync(0xffffffffu, c0, 0);
+                if (c0 >= featCount) return -1;
+                qBase = c0;
+                const int k = min(kSweepChunk, featCount - c0);
+                qMask = (1u << k) - 1u;
+            }
+            runMin = fminf(runMin, __uint_as_float(*runMinBits));
+            const float lim = __fadd_ru(runMin, window);
+            const bool mine = lane < kSweepChunk && ((qMask >> lane) & 1u);
+            bool keep = false, used = false;
+            float bound = 0.0f;
+            if (mine) {
+                const int c = qBase + lane;
+                used = usedMask != nullptr && usedMask[c] != 0;
+                if (prune) bound = __fmul_rd(lb[c], scale);
+                keep = !used && !(bound > lim);
+            }
+            const unsigned km = __ballot_sync(0xffffffffu, keep);
+            const int first = km ? __ffs(km) - 1 : 32;
+            // the chunk's features before the first one kept are not streamed;
+            // their bounds (also those of used features, which a caller may
+            // clear later) carry over to the next round
+            if (mine && lane < first) {
+                const int c = qBase + lane;
+                fastErr[c] = INFINITY;
+                lb[c] = bound;
+            }
+            if (km) {
+                qMask &= ~((2u << first) - 1u);
+                return qBase + first;
+            }
+            qMask = 0;
+        }
+    };
+    // Used features are skipped when reached, so no load waits on the mask.
+    auto load = [&](int f, int t, uint4& a, uint4& b, uint32_t& g) {
         a = b = make_uint4(z, z, z, z);
         g = 0;
-        if (it >= items) return;
+        if (f < 0) return;
         const int k0 = lane * L + 16 * t;
         const uint16_t* row = ord + static_cast<size_t>(f) * ordStride + 512 * t + lane * 8;  // ord_slot(k0, L)
         if (k0 < n) a = __ldg(reinterpret_cast<const uint4*>(row));
         if (k0 + 8 < n) b = __ldg(reinterpret_cast<const uint4*>(row + 256));
         if (k0 < n - 1) g = __ldg(gap + static_cast<size_t>(f) * gapStride + 32 * t + lane);  // gap_word(k0, L)
     };
-    float blockMin = INFINITY;
+    auto advance = [&](int& f, int& t) {
+        if (f < 0) return;
+        if (++t == spf) {
+            t = 0;
+            f = next_feature();
+        }
+    };
+    int f = next_feature(), t = 0;  // item being processed
+    int fn = f, tn = t;             // item being loaded
+    advance(fn, tn);
     uint4 ca, cb;
     uint32_t cg;
-    int f = gw, t = 0;     // item being processed
-    int fn = gw, tn = 1;   // item being loaded
-    if (tn == spf) {
-        tn = 0;
-        fn += nw;
-    }
-    load(0, f, t, ca, cb, cg);
+    load(f, t, ca, cb, cg);
     float carry = 0.0f, comp = 0.0f, pmin = INFINITY, pmax = -INFINITY;
-    for (int it = 0; it < items; ++it) {
+    while (f >= 0) {
         uint4 na, nb;
         uint32_t ng;
-        load(it + 1, fn, tn, na, nb, ng);
-        if (++tn == spf) {
-            tn = 0;
-            fn += nw;
-        }
+        load(fn, tn, na, nb, ng);
+        int fa = fn, ta = tn;  // the item after the one being loaded
+        advance(fa, ta);
         const uint32_t w8[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
         float s = 0.0f, lmin = INFINITY, lmax = -INFINITY;
 #pragma unroll
@@ -724,29 +822,31 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
                 hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
             }
             float best = INFINITY;
-            if (hi > -INFINITY && !(usedMask && usedMask[f]))
-                best = fmaxf(fminf(__fsub_rn(TP, hi), __fadd_rn(TN, lo)), 0.0f);
-            if (lane == 0) fastErr[f] = best;
-            blockMin = fminf(blockMin, best);
+            if (hi > -INFINITY) best = fmaxf(fminf(__fsub_rn(TP, hi), __fadd_rn(TN, lo)), 0.0f);
+            if (lane == 0) {
+                fastErr[f] = best;
+                // exact best error >= fast error - bfast; +inf for no valid split,
+                // which no later round of the stage can change
+                lb[f] = fmaxf(__fsub_rd(best, bfast), 0.0f);
+                if (best < runMin) atomicMin(&prm->fastMinBits, __float_as_uint(best));
+                ++swept;
+            }
+            runMin = fminf(runMin, best);
             carry = comp = 0.0f;
             pmin = INFINITY;
             pmax = -INFINITY;
         }
-        if (++t == spf) {
-            t = 0;
-            f += nw;
-        }
+        f = fn;
+        t = tn;
+        fn = fa;
+        tn = ta;
         ca = na;
         cb = nb;
         cg = ng;
     }
-    __shared__ float wmin[kSweepWarps];
-    if (lane == 0) wmin[threadIdx.x >> 5] = blockMin;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float m = INFINITY;
-        for (int k = 0; k < kSweepWarps; ++k) m = fminf(m, wmin[k]);
-        if (m < INFINITY) atomicMin(&prm->fastMinBits, __float_as_uint(m));
+    if (lane == 0 && swept) {
+        atomicAdd(&prm->swept, swept);
+        atomicAdd(sweptTotal, static_cast<unsigned long long>(swept));
     }
 }
 
@@ -1007,7 +1107,8 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
                     const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
                     const float* __restrict__ weight, float* __restrict__ strong, int n,
                     uint8_t* __restrict__ usedMask, vj_weak_classifier* __restrict__ weakOut,
-                    int* __restrict__ status, double* __restrict__ xbuf, double* __restrict__ partials, int* gate) {
+                    int* __restrict__ status, double* __restrict__ xbuf, double* __restrict__ partials,
+                    PruneState* __restrict__ ps, int* gate) {
     if (gate_closed(gate)) return;
     __shared__ vj_haar_feature sfeat;
     __shared__ float sTheta, sLeft, sRight;
@@ -1024,6 +1125,7 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
             const double ed = static_cast<double>(e);
             const float C = static_cast<float>(log((1.0 - ed) / ed));
             sF = exp(static_cast<double>(C));
+            if (ps && blockIdx.x == 0) ps->F = sF;
             sTheta = b.bestTheta;
             sPar = b.bestParity;
             sLeft = b.bestParity > 0 ? -C : C;
@@ -1075,9 +1177,15 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
     partials[t] = acc;
 }
 
+// With wShadow given, the new weights are also written there, and block 0
+// records the factor that takes a feature's exact error under the old weights
+// to a lower bound under the new ones: every new weight is at least
+// min(1, F) / Z times the old one, up to the FP32 rounding of the division
+// (relative 2^-24, covered by the factor 1 - 4u).
 __global__ void __launch_bounds__(256)
 round_normalize_kernel(const vj_tile_best* __restrict__ best, const double* __restrict__ xbuf,
-                       const double* __restrict__ partials, float* __restrict__ weight, int n, const int* gate) {
+                       const double* __restrict__ partials, float* __restrict__ weight, int n,
+                       float* __restrict__ wShadow, PruneState* __restrict__ ps, const int* gate) {
     if (gate_closed(gate)) return;
     if (!best_valid(*best)) return;
     __shared__ double part[kRoundPartials];
@@ -1090,7 +1198,15 @@ round_normalize_kernel(const vj_tile_best* __restrict__ best, const double* __re
     const double Z = part[0];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double x = xbuf[i];
-        weight[i] = (Z > 1e-30) ? static_cast<float>(x / Z) : static_cast<float>(x);
+        const float w = (Z > 1e-30) ? static_cast<float>(x / Z) : static_cast<float>(x);
+        weight[i] = w;
+        if (wShadow) wShadow[i] = w;
+    }
+    if (ps && blockIdx.x == 0 && threadIdx.x == 0) {
+        const double u = 5.9604644775390625e-08;
+        const double g = (Z > 1e-30) ? fmin(1.0, ps->F) / Z * (1.0 - 4.0 * u) : 0.0;
+        ps->scale = __double2float_rd(fmin(g, 1.0));
+        ps->valid = g > 0.0 ? 1 : 0;
     }
 }
 
@@ -1441,6 +1557,16 @@ struct vj_trainer {
     int* d_refSplit = nullptr;
     RoundParams* d_prm = nullptr;
     int* d_status = nullptr;
+    // Sweep pruning: per-feature lower bounds of the exact best error, the
+    // weights as the last round update left them, the active mask as the last
+    // search saw it, and the last update's factor; reset (no pruning in the
+    // next search) whenever the training set, the pool or the range changes.
+    float* d_lb = nullptr;
+    float* d_wShadow = nullptr;
+    uint8_t* d_aShadow = nullptr;
+    PruneState* d_prune = nullptr;
+    bool pruneReset = true;
+    unsigned long long* d_sweptTotal = nullptr;  // features streamed since the trainer was created
     int* d_gate = nullptr;  // stage gate of the round kernels (caller's memory), or none
     int64_t scratchFeat = 0;
     int scratchN = 0;
@@ -1459,6 +1585,11 @@ int ensure_round_scratch(vj_trainer* t) {
     cudaFree(t->d_prefix);
     cudaFree(t->d_refParity);
     cudaFree(t->d_refSplit);
+    cudaFree(t->d_lb);
+    cudaFree(t->d_wShadow);
+    cudaFree(t->d_aShadow);
+    t->d_lb = t->d_wShadow = nullptr;
+    t->d_aShadow = nullptr;
     t->d_wsg = nullptr;
     t->d_fastErr = nullptr;
     t->d_cand = nullptr;
@@ -1480,6 +1611,15 @@ int ensure_round_scratch(vj_trainer* t) {
     VJ_CUDA_TRY(cudaMalloc(&t->d_prefix, sizeof(float2) * static_cast<size_t>(refine_blocks()) * kRefineWarps * N));
     VJ_CUDA_TRY(cudaMalloc(&t->d_refParity, F));
     VJ_CUDA_TRY(cudaMalloc(&t->d_refSplit, sizeof(int) * F));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_lb, sizeof(float) * F));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_wShadow, sizeof(float) * N));
+    VJ_CUDA_TRY(cudaMalloc(&t->d_aShadow, N));
+    if (!t->d_prune) VJ_CUDA_TRY(cudaMalloc(&t->d_prune, sizeof(PruneState)));
+    if (!t->d_sweptTotal) {
+        VJ_CUDA_TRY(cudaMalloc(&t->d_sweptTotal, sizeof(unsigned long long)));
+        VJ_CUDA_TRY(cudaMemset(t->d_sweptTotal, 0, sizeof(unsigned long long)));
+    }
+    t->pruneReset = true;
     if (!t->d_prm) VJ_CUDA_TRY(cudaMalloc(&t->d_prm, sizeof(RoundParams)));
     if (!t->d_status) VJ_CUDA_TRY(cudaMalloc(&t->d_status, sizeof(int)));
     t->scratchFeat = F;
@@ -1585,6 +1725,11 @@ int vj_trainer_destroy(vj_trainer* t) {
     cudaFree(t->d_status);
     cudaFree(t->d_sortKeys);
     cudaFree(t->d_sortIdx);
+    cudaFree(t->d_lb);
+    cudaFree(t->d_wShadow);
+    cudaFree(t->d_aShadow);
+    cudaFree(t->d_prune);
+    cudaFree(t->d_sweptTotal);
     delete t;
     return ok();
 }
@@ -1614,6 +1759,7 @@ int vj_trainer_set_features(vj_trainer* t, const vj_haar_feature* features, int6
     t->rangeBegin = 0;
     t->rangeCount = -1;
     t->prepared = false;
+    t->pruneReset = true;
     VJ_CUDA_TRY(cudaMalloc(&t->d_feat, sizeof(vj_haar_feature) * count));
     VJ_CUDA_TRY(cudaMemcpy(t->d_feat, features, sizeof(vj_haar_feature) * count, cudaMemcpyHostToDevice));
     t->nFeat = count;
@@ -1633,6 +1779,7 @@ int vj_trainer_bind(vj_trainer* t, const uint32_t* d_sumT, const float* d_invNor
     t->d_active = d_active;
     t->d_weight = d_weight;
     t->prepared = false;
+    t->pruneReset = true;
     return ok();
 }
 
@@ -1647,6 +1794,11 @@ int vj_trainer_last_round(vj_trainer* t, vj_round_info* out) {
     out->status = p.status;
     out->totalPos = p.tp;
     out->totalNeg = p.tn;
+    out->swept = p.swept;
+    out->pad0 = 0;
+    unsigned long long total = 0;
+    VJ_CUDA_TRY(cudaMemcpy(&total, t->d_sweptTotal, sizeof(total), cudaMemcpyDeviceToHost));
+    out->sweptTotal = static_cast<int64_t>(total);
     // the two smallest (error, featureIdx) keys among the exactly replayed candidates
     out->bestFeature = out->runnerUpFeature = -1;
     out->bestErr = out->runnerUpErr = INFINITY;
@@ -1684,6 +1836,7 @@ int vj_trainer_prepare_stage(vj_trainer* t, void* stream) {
     st = sort_all(t, static_cast<cudaStream_t>(stream));
     if (st != VJ_OK) return st;
     t->prepared = true;
+    t->pruneReset = true;
     return ok();
 }
 
@@ -1694,6 +1847,7 @@ int vj_trainer_set_search_range(vj_trainer* t, int64_t featureBegin, int64_t fea
     t->rangeBegin = featureBegin;
     t->rangeCount = featureCount;
     t->prepared = false;
+    t->pruneReset = true;
     return ok();
 }
 
@@ -1725,9 +1879,13 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
     const int F = static_cast<int>(range_count(t)), n = t->n;
     const int fb = static_cast<int>(range_begin(t));
     const uint8_t* usedRange = d_usedMask ? d_usedMask + fb : nullptr;
+    if (t->pruneReset) {
+        VJ_CUDA_TRY(cudaMemsetAsync(t->d_prune, 0, sizeof(PruneState), s));
+        t->pruneReset = false;
+    }
     VJ_TIMED_LAUNCH("prep_round_kernel", s,
                     prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, n, t->d_wsg, t->d_prm,
-                                                         t->d_gate));
+                                                         t->d_wShadow, t->d_aShadow, t->d_prune, t->d_gate));
     VJ_LAUNCH_CHECK("prep_round_kernel");
     const bool smemW = n <= kSmemWeightsMax;
     const int sb = t->slotBase;
@@ -1742,7 +1900,8 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
         VJ_TIMED_LAUNCH("sweep_kernel", s,
                         k<<<grid, tpb, wbytes, s>>>(t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb,
-                                                    t->laneRun, F, usedRange, t->d_prm, t->d_fastErr, t->d_gate));
+                                                    t->laneRun, F, usedRange, t->d_prm, t->d_fastErr, t->d_lb,
+                                                    t->d_sweptTotal, t->d_gate));
         VJ_LAUNCH_CHECK("sweep_kernel");
     }
     VJ_TIMED_LAUNCH("select_candidates_kernel", s,
@@ -1780,11 +1939,13 @@ int vj_round_update(vj_trainer* t, const vj_tile_best* d_best, float* d_strong, 
     VJ_TIMED_LAUNCH("round_update_kernel", s,
                     round_update_kernel<<<kRoundUpdateCtas, 256, 0, s>>>(
                         t->d_feat, d_best, t->d_sumT, t->d_invNorm, t->d_label, t->d_active, t->d_weight, d_strong,
-                        t->n, d_usedMask, d_weak_out, t->d_status, t->d_xbuf, t->d_partials, t->d_gate));
+                        t->n, d_usedMask, d_weak_out, t->d_status, t->d_xbuf, t->d_partials, t->d_prune,
+                        t->d_gate));
     VJ_LAUNCH_CHECK("round_update_kernel");
     VJ_TIMED_LAUNCH("round_normalize_kernel", s,
                     round_normalize_kernel<<<std::min(div_up(t->n, 256), 2 * sm_count()), 256, 0, s>>>(
-                        d_best, t->d_xbuf, t->d_partials, t->d_weight, t->n, t->d_gate));
+                        d_best, t->d_xbuf, t->d_partials, t->d_weight, t->n, t->d_wShadow, t->d_prune,
+                        t->d_gate));
     VJ_LAUNCH_CHECK("round_normalize_kernel");
     return ok();
 }
@@ -1840,7 +2001,7 @@ int vj_trainer_find_thresholds(vj_trainer* t, const float* d_resp, const uint16_
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VJ_TIMED_LAUNCH("prep_round_kernel", s,
                     prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, t->n, t->d_wsg,
-                                                         t->d_prm, nullptr));
+                                                         t->d_prm, nullptr, nullptr, nullptr, nullptr));
     VJ_LAUNCH_CHECK("prep_round_kernel");
     VJ_TIMED_LAUNCH("find_thresholds_kernel", s,
                     find_thresholds_kernel<<<div_up(featureCount, 8), 256, 0, s>>>(d_resp, d_sortedIdx, t->n,

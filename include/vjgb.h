@@ -321,7 +321,11 @@ int vj_reduce_tile_best(const vj_tile_best* d_in, int count, vj_tile_best* d_out
  * smallest exact (reference-replayed FP32) errors among the candidates - the
  * pick and its runner-up (runnerUpFeature -1 and runnerUpErr +inf when the pick
  * was the only candidate: every other feature's fast error exceeded the pick's
- * by more than the window).  Copies from the device after synchronising. */
+ * by more than the window).  `swept` counts the features whose orders the
+ * search streamed: from the second round of a stage on, features whose error
+ * bound shows they cannot reach the candidate window are skipped (the pick is
+ * unchanged; bounds are used only while the weights change by
+ * vj_round_update alone).  Copies from the device after synchronising. */
 typedef struct {
     float fastMin;
     float window;
@@ -333,6 +337,9 @@ typedef struct {
     int32_t bestFeature;
     float runnerUpErr;
     int32_t runnerUpFeature;
+    int32_t swept;       /* features the sweep streamed (the others were pruned or used) */
+    int32_t pad0;
+    int64_t sweptTotal;  /* features streamed by every search of this trainer so far */
 } vj_round_info;
 
 int vj_trainer_last_round(vj_trainer* t, vj_round_info* out);

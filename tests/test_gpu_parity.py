@@ -618,3 +618,51 @@ def test_tilted_features_like_the_reference(cuda, vj, oracle, golden, gin):
     s, grp = e.detectMultiScale(scene, 200, 150, 200, 1.25, 4, 24, 200000)
     assert s == 0 and as_set(grp) == as_set(gin["tdet_grouped"])
     assert grp.tobytes() == oracle.group_first_order(raw, 4, 0.2).tobytes()
+
+
+# ---------------------------------------------------------------- sweep pruning
+def test_pruned_sweep_rounds_equal_oracle_and_fresh_searches(cuda, vj, oracle, basic_pool):
+    """Within a stage the sweep skips features whose error bound (last round's
+    error times the update's factor) cannot reach the candidate window.  Ten
+    rounds with the resident orders: every pick equals the oracle's and that
+    of a fresh search (a new bind, so nothing is pruned), and some round
+    actually skips features.  Weights edited outside vj_round_update between
+    two rounds turn the pruning off for that round (the pick still equals the
+    oracle's), as does clearing a used-mask entry."""
+    torch = cuda
+    npos = nneg = 2000
+    p = vj.synth_patches(71, npos, nneg)
+    labels = np.array([1] * npos + [-1] * nneg, np.int8)
+    feats = np.ascontiguousarray(basic_pool[::7])
+    n, F = len(labels), len(feats)
+    w0 = np.full(n, np.float32(0.5) / np.float32(npos), np.float32)
+    T = Train(cuda, vj, oracle, p, labels, feats, w0)
+    assert T.t.prepareStage() == 0
+    sums, inv = oracle.train_integrals(p)
+    used = np.zeros(F, np.uint8)
+    weak = cuda.zeros(7, dtype=cuda.int32, device="cuda")
+    swept = []
+    rng = np.random.default_rng(5)
+    for r in range(10):
+        if r == 6:  # an edit outside the round update
+            w = T.w.cpu().numpy() * (1.0 + 0.01 * rng.random(n)).astype(np.float32)
+            T.w.copy_(torch.from_numpy((w / w.sum(dtype=np.float64)).astype(np.float32)))
+        if r == 8:  # a used feature cleared again
+            f_clear = int(np.nonzero(used)[0][0])
+            used[f_clear] = 0
+            T.used[f_clear] = 0
+        got = T.search(used=True)
+        swept.append(T.t.lastRound()["swept"])
+        w = T.w.cpu().numpy()
+        ref = oracle.weak_search(feats, sums, inv, labels, w, used=used, threads=16)
+        assert got == (ref["featureIdx"], ref["err"], ref["theta"], ref["parity"]), r
+        fresh = Train(cuda, vj, oracle, p, labels, feats, w)
+        assert fresh.t.prepareStage() == 0
+        fresh.used.copy_(T.used)
+        assert fresh.search(used=True) == got, r
+        assert fresh.t.lastRound()["swept"] == F - int(used.sum())  # a fresh bind prunes nothing
+        assert T.t.applyBestWeak(T.best, T.strong, T.used, weak) == 0
+        used[got[0]] = 1
+    assert swept[0] == F  # the first search of a stage has no bounds yet
+    assert swept[6] == F - 6  # the edited weights: every unused feature streamed
+    assert min(swept[1:6]) < F // 2, swept  # bounds skip most features in some round
