@@ -238,6 +238,74 @@ constexpr size_t sort_smem_bytes() {
     return static_cast<size_t>(1024 * R) * (4 + (sort_ping_pong<R>() ? 4 : 2)) + 256 * kCntStride * 4;
 }
 
+// Outputs of one sorted feature (every thread of the 1024-thread CTA calls
+// this after the last pass): the split bitmask from the sorted keys (keys[]
+// in sample order, idx[] the sorted sample order; gnat is scratch for n/32
+// words), the two-copy slot assignment, and the order row, in the lane-run
+// layout when ordPadded.  idx[] is rewritten in place (slots, padding).
+__device__ __forceinline__ void sort_epilogue(const uint32_t* keys, uint16_t* idx, uint32_t* gnat, int n, int fl,
+                                              uint16_t* __restrict__ ordOut, int64_t ordStride, bool ordPadded,
+                                              uint16_t* __restrict__ gapOut, int64_t gapStride, int slotBase, int L) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gapWords = (n + 31) >> 5;
+    // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
+    // A warp takes 32 consecutive positions per step, one per lane; the
+    // next value comes from the next lane, and the word from one ballot.
+    // The words (in the free digit-counter array) are then stored in the
+    // lane-run layout of the resident orders (see ord_slot).
+    if (gapOut) {
+        for (int k0 = warp * 32; k0 < gapWords * 32; k0 += kSortThreads) {
+            const int k = k0 + lane;
+            const float v0 = k < n ? __uint_as_float(radix_key_inv(keys[idx[k]])) : 0.0f;
+            float v1 = __shfl_down_sync(0xffffffffu, v0, 1);
+            if (lane == 31 && k + 1 < n) v1 = __uint_as_float(radix_key_inv(keys[idx[k + 1]]));
+            const uint32_t bits = __ballot_sync(0xffffffffu, k + 1 < n && __fadd_rn(v0, 1e-7f) < v1);
+            if (lane == 0) gnat[k0 >> 5] = bits;
+        }
+        __syncthreads();
+        uint16_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
+        for (int j = tid; j < 2 * L; j += kSortThreads) {
+            const int k = (j & 31) * L + 16 * (j >> 5);  // first position of the word
+            grow[j] = k < n ? static_cast<uint16_t>(gnat[k >> 5] >> (k & 31)) : uint16_t(0);
+        }
+    }
+    // Two weight copies: pick each position's copy.  The sweep's gather
+    // instruction i of step t reads positions m*L + 16t + i, m = 0..31
+    // (lane m); one thread takes that group and assigns its members in
+    // turn to the less loaded of their two banks (greedy two-choice, loads
+    // tracked up to 2 in two bit masks: o1 = banks with load >= 1, o2 = >= 2).
+    if (ordPadded && slotBase > 0) {
+        __syncthreads();
+        for (int g = tid; g < L; g += kSortThreads) {
+            const int kb = 16 * (g >> 4) + (g & 15);
+            uint32_t o1 = 0, o2 = 0;
+            for (int m = 0; m < 32 && kb + m * L < n; ++m) {
+                const uint32_t id = idx[kb + m * L];
+                const uint32_t off1 = copy1_offset(id);
+                const int b0 = id & 31, b1 = off1 & 31;
+                // copy 1 is less loaded: b0 at 1 and b1 empty, or b0 at 2 and b1 below 2
+                const bool one = ((o1 >> b0) & 1u) && !((((o2 >> b0) & 1u) ? o2 : o1) >> b1 & 1u);
+                const uint32_t bit = 1u << (one ? b1 : b0);
+                o2 |= o1 & bit;
+                o1 |= bit;
+                if (one) idx[kb + m * L] = static_cast<uint16_t>(slotBase + off1);
+            }
+        }
+        __syncthreads();
+    }
+    // Sorted sample order (padded rows: lane runs, see ord_slot).
+    uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
+    if (ordPadded) {
+        const int n8 = (n + 7) & ~7;
+        if (tid < n8 - n) idx[n + tid] = static_cast<uint16_t>(zero_slot(n, slotBase));
+        __syncthreads();
+        for (int k = tid * 8; k < n8; k += kSortThreads * 8)
+            *reinterpret_cast<uint4*>(orow + ord_slot(k, L)) = *reinterpret_cast<const uint4*>(idx + k);
+    } else {
+        for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
+    }
+}
+
 template <int R, bool kFromResp>
 __global__ void __launch_bounds__(kSortThreads, 1)
 eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int featCount,
@@ -254,7 +322,6 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
     __shared__ uint32_t warpTot[32];
     __shared__ vj_haar_feature sfeat;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int gapWords = (n + 31) >> 5;
 
     for (int fl = blockIdx.x; fl < featCount; fl += gridDim.x) {
         if (kFromResp) {
@@ -346,63 +413,167 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
             __syncthreads();
         }
 
-        // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
-        // A warp takes 32 consecutive positions per step, one per lane; the
-        // next value comes from the next lane, and the word from one ballot.
-        // The words (in the free digit-counter array) are then stored in the
-        // lane-run layout of the resident orders (see ord_slot).
-        if (gapOut) {
-            uint32_t* gnat = cnt;
-            for (int k0 = warp * 32; k0 < gapWords * 32; k0 += kSortThreads) {
-                const int k = k0 + lane;
-                const float v0 = k < n ? __uint_as_float(radix_key_inv(keys[idx[k]])) : 0.0f;
-                float v1 = __shfl_down_sync(0xffffffffu, v0, 1);
-                if (lane == 31 && k + 1 < n) v1 = __uint_as_float(radix_key_inv(keys[idx[k + 1]]));
-                const uint32_t bits = __ballot_sync(0xffffffffu, k + 1 < n && __fadd_rn(v0, 1e-7f) < v1);
-                if (lane == 0) gnat[k0 >> 5] = bits;
-            }
+        sort_epilogue(keys, idx, cnt, n, fl, ordOut, ordStride, ordPadded, gapOut, gapStride, slotBase, L);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 1c. The evaluate + stable LSD radix sort with per-thread digit counters, for
+//     n <= 1024 * kBlockedMaxR samples.  In every pass thread t takes the R
+//     consecutive items [tR, tR + R) of the current sequence (a blocked
+//     arrangement), so an item's rank among the thread's items with the same
+//     digit is a count the thread keeps itself and no ballot is needed.
+//     Digits are 5 bits (32 values); the counters are 16-bit halves of
+//     shared-memory words, word row c holding digits c and c + 16 of every
+//     thread, and the 32 threads of a warp always touch 32 different banks.
+//     An exclusive scan of the counters in (digit, thread) order gives every
+//     (digit, thread) pair its first output position; the scatter takes the
+//     items again in order and bumps the pair's position per item, so equal
+//     digits keep sequence order (stable) and the final order is
+//     eval_sort_kernel's.  Seven passes (the last of 2 bits) cover the 32-bit
+//     keys.  Positions n..NP-1 carry the largest key, so they stay last.
+// ---------------------------------------------------------------------------
+constexpr int kDigitBits = 5;
+constexpr int kDigitPasses = 7;
+constexpr int kCntRows = 16;          // 32 digits, two 16-bit counters a word
+constexpr int kCntRow = 1024 + 32;    // a row of 1024 thread words, one pad word per 32
+constexpr int kBlockedMaxR = 20;
+
+template <int R>
+constexpr size_t blocked_sort_smem_bytes() {
+    return static_cast<size_t>(1024 * R) * (4 + 2 + 2) + static_cast<size_t>(kCntRows) * kCntRow * 4 + 16;
+}
+
+// Exclusive scan, in place, of the per-thread digit counters in (row, thread)
+// order, both halves at once: every total stays below 2^16, so the low halves
+// (digits 0..15) never carry into the high ones; the low halves' total is then
+// added to every high half, since digits 16..31 follow all of digits 0..15.
+// Thread t takes the 16 consecutive words [16t, 16t + 16) of that order; with
+// one pad word per 32, the 32 lanes of a warp read 32 different banks.
+__device__ __forceinline__ void scan_thread_counters(uint32_t* cnt, uint32_t* warpTot, uint32_t* blockTotal) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int t0 = (tid & 63) * 16;
+    uint32_t* base = cnt + (tid >> 6) * kCntRow + t0 + (t0 >> 5);
+    uint32_t v[16];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        v[k] = base[k];
+        sum += v[k];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warpTot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t t = warpTot[lane];
+        uint32_t x = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        warpTot[lane] = x - t;
+        if (lane == 31) *blockTotal = x;
+    }
+    __syncthreads();
+    uint32_t run = warpTot[warp] + incl - sum + ((*blockTotal & 0xFFFFu) << 16);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        base[k] = run;
+        run += v[k];
+    }
+}
+
+template <int R, bool kFromResp>
+__global__ void __launch_bounds__(kSortThreads, 1)
+eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int featCount,
+                         const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm, int n,
+                         const float* __restrict__ resp, uint16_t* __restrict__ ordOut, int64_t ordStride,
+                         bool ordPadded, uint16_t* __restrict__ gapOut, int64_t gapStride, int slotBase, int L) {
+    static_assert(R % 2 == 0 && R <= kBlockedMaxR, "an even number of items per thread, at most kBlockedMaxR");
+    constexpr int NP = 1024 * R;
+    constexpr int kPk = (R + 5) / 6;  // words of six 5-bit digits
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);     // radix keys in sample order
+    uint16_t* idxA = reinterpret_cast<uint16_t*>(keys + NP);
+    uint16_t* idxB = idxA + NP;                              // the sorted order after the last pass
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(idxB + NP);  // [kCntRows][kCntRow]
+    uint32_t* blockTotal = cnt + kCntRows * kCntRow;
+    __shared__ uint32_t warpTot[32];
+    __shared__ vj_haar_feature sfeat;
+    const int tid = threadIdx.x;
+    uint32_t* ccol = cnt + tid + (tid >> 5);  // this thread's counter word of row 0
+
+    for (int fl = blockIdx.x; fl < featCount; fl += gridDim.x) {
+        if (kFromResp) {
+            const float* row = resp + static_cast<size_t>(fl) * n;
+            for (int s = tid; s < NP; s += kSortThreads) keys[s] = s < n ? radix_key(__float_as_uint(row[s])) : ~0u;
+        } else {
+            if (tid == 0) sfeat = feats[featBegin + fl];
             __syncthreads();
-            uint16_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
-            for (int j = tid; j < 2 * L; j += kSortThreads) {
-                const int k = (j & 31) * L + 16 * (j >> 5);  // first position of the word
-                grow[j] = k < n ? static_cast<uint16_t>(gnat[k >> 5] >> (k & 31)) : uint16_t(0);
+            const vj_haar_feature& f = sfeat;
+            for (int s0 = tid; s0 < NP; s0 += 4 * kSortThreads) {
+                float r[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int s = s0 + u * kSortThreads;
+                    r[u] = s < n ? train_response(f, sumT, n, s, __ldg(invNorm + s)) : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int s = s0 + u * kSortThreads;
+                    if (s < NP) keys[s] = s < n ? radix_key(__float_as_uint(r[u])) : ~0u;
+                }
             }
         }
-        // Two weight copies: pick each position's copy.  The sweep's gather
-        // instruction i of step t reads positions m*L + 16t + i, m = 0..31
-        // (lane m); one thread takes that group and assigns its members in
-        // turn to the less loaded of their two banks (greedy two-choice, loads
-        // tracked up to 2 in two bit masks: o1 = banks with load >= 1, o2 = >= 2).
-        if (ordPadded && slotBase > 0) {
+        __syncthreads();
+
+        for (int pass = 0; pass < kDigitPasses; ++pass) {
+            const int shift = pass * kDigitBits;
+            // pass 0 takes the sample order; even passes write B, odd ones A
+            const uint32_t* src2 = reinterpret_cast<const uint32_t*>((pass & 1) ? idxB : idxA) + tid * (R / 2);
+            uint16_t* dst = (pass & 1) ? idxA : idxB;
+#pragma unroll
+            for (int c = 0; c < kCntRows; ++c) ccol[c * kCntRow] = 0;
+            uint32_t dg[kPk];
+#pragma unroll
+            for (int c = 0; c < kPk; ++c) dg[c] = 0;
+#pragma unroll
+            for (int j = 0; j < R; j += 2) {
+                const uint32_t two = pass == 0 ? static_cast<uint32_t>(tid * R + j) * 0x10001u + 0x10000u : src2[j / 2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t id = h ? two >> 16 : two & 0xFFFFu;
+                    const uint32_t d = (keys[id] >> shift) & 31u;
+                    ccol[(d & 15u) * kCntRow] += 1u << (d & 16u);
+                    dg[(j + h) / 6] |= d << (5 * ((j + h) % 6));
+                }
+            }
             __syncthreads();
-            for (int g = tid; g < L; g += kSortThreads) {
-                const int kb = 16 * (g >> 4) + (g & 15);
-                uint32_t o1 = 0, o2 = 0;
-                for (int m = 0; m < 32 && kb + m * L < n; ++m) {
-                    const uint32_t id = idx[kb + m * L];
-                    const uint32_t off1 = copy1_offset(id);
-                    const int b0 = id & 31, b1 = off1 & 31;
-                    // copy 1 is less loaded: b0 at 1 and b1 empty, or b0 at 2 and b1 below 2
-                    const bool one = ((o1 >> b0) & 1u) && !((((o2 >> b0) & 1u) ? o2 : o1) >> b1 & 1u);
-                    const uint32_t bit = 1u << (one ? b1 : b0);
-                    o2 |= o1 & bit;
-                    o1 |= bit;
-                    if (one) idx[kb + m * L] = static_cast<uint16_t>(slotBase + off1);
+            scan_thread_counters(cnt, warpTot, blockTotal);
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < R; j += 2) {
+                const uint32_t two = pass == 0 ? static_cast<uint32_t>(tid * R + j) * 0x10001u + 0x10000u : src2[j / 2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t id = h ? two >> 16 : two & 0xFFFFu;
+                    const uint32_t d = (dg[(j + h) / 6] >> (5 * ((j + h) % 6))) & 31u;
+                    uint32_t* cw = ccol + (d & 15u) * kCntRow;
+                    const uint32_t w = *cw;
+                    *cw = w + (1u << (d & 16u));
+                    dst[(w >> (d & 16u)) & 0xFFFFu] = static_cast<uint16_t>(id);
                 }
             }
             __syncthreads();
         }
-        // Sorted sample order (padded rows: lane runs, see ord_slot).
-        uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
-        if (ordPadded) {
-            const int n8 = (n + 7) & ~7;
-            if (tid < n8 - n) idx[n + tid] = static_cast<uint16_t>(zero_slot(n, slotBase));
-            __syncthreads();
-            for (int k = tid * 8; k < n8; k += kSortThreads * 8)
-                *reinterpret_cast<uint4*>(orow + ord_slot(k, L)) = *reinterpret_cast<const uint4*>(idx + k);
-        } else {
-            for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
-        }
+        sort_epilogue(keys, idxB, cnt, n, fl, ordOut, ordStride, ordPadded, gapOut, gapStride, slotBase, L);
         __syncthreads();
     }
 }
@@ -1497,7 +1668,9 @@ int launch_eval_sort(const vj_haar_feature* feats, int featBegin, int featCount,
     VJ_SORT_CASE(4)
     VJ_SORT_CASE(8)
     VJ_SORT_CASE(16)
-    VJ_SORT_CASE(20)
+    if (n <= 1024 * kBlockedMaxR)
+        return resp ? go(eval_sort_blocked_kernel<kBlockedMaxR, true>, blocked_sort_smem_bytes<kBlockedMaxR>())
+                    : go(eval_sort_blocked_kernel<kBlockedMaxR, false>, blocked_sort_smem_bytes<kBlockedMaxR>());
     VJ_SORT_CASE(24)
     VJ_SORT_CASE(32)
 #undef VJ_SORT_CASE

@@ -122,12 +122,13 @@ def test_weak_search_resident_equals_fused(cuda, vj, oracle, gin, basic_pool):
     assert T.search() == fused
 
 
-@pytest.mark.parametrize("n", [24576, 25600, 32768])
+@pytest.mark.parametrize("n", [16385, 20000, 20480, 24576, 25600, 32768])
 def test_weak_search_both_weight_layouts(cuda, vj, oracle, basic_pool, n):
     """Up to 24,576 samples the resident orders carry slots of two bank-spread
     weight copies; above that one copy and plain sample indices, up to the
-    on-chip sort's maximum of 32,768.  All give the oracle's pick, round after
-    round."""
+    on-chip sort's maximum of 32,768.  From 16,385 to 20,480 samples the sort
+    is the blocked form with per-thread digit counters.  All give the oracle's
+    pick, round after round."""
     p = vj.synth_patches(31, n // 2, n // 2)
     labels = np.array([1] * (n // 2) + [-1] * (n // 2), np.int8)
     feats = np.ascontiguousarray(basic_pool[::317][:512])
@@ -176,14 +177,18 @@ def test_weak_search_beyond_on_chip_sort(cuda, vj, oracle, basic_pool, n, with_a
         used[got[0]] = 1
 
 
-def test_step_api_sort_beyond_on_chip_sort(cuda, vj, oracle, basic_pool):
-    """sortSamplesPerFeature at 40,001 samples: the stable order of the radix
-    keys, -0.0 before +0.0 (a flat patch has invNorm 0)."""
+@pytest.mark.parametrize("n", [16385, 18001, 20480, 40001])
+def test_step_api_sort_beyond_on_chip_sort(cuda, vj, oracle, basic_pool, n):
+    """sortSamplesPerFeature at 16,385 to 20,480 samples (the blocked sort with
+    per-thread digit counters) and at 40,001 (keys and indices in a global
+    scratch): the stable order of the radix keys, -0.0 before +0.0 (a flat
+    patch has invNorm 0)."""
     torch = cuda
-    n, F = 40001, 40
-    p = vj.synth_patches(63, 20000, n - 20000)
+    F = 40
+    npos = n // 2
+    p = vj.synth_patches(63, npos, n - npos)
     p[11] = 77  # flat: responses +-0.0
-    labels = np.array([1] * 20000 + [-1] * (n - 20000), np.int8)
+    labels = np.array([1] * npos + [-1] * (n - npos), np.int8)
     feats = np.ascontiguousarray(basic_pool[::4001][:F])
     T = Train(cuda, vj, oracle, p, labels, feats, np.full(n, np.float32(1.0 / n), np.float32))
     resp = torch.empty(F * n, dtype=torch.float32, device="cuda")
