@@ -259,6 +259,26 @@ __device__ __forceinline__ void resize_item(const ResizeJob* __restrict__ jobs, 
 // Window evaluation.
 // ---------------------------------------------------------------------------
 
+// float(1 / sqrt(x)) with the reference's rounding - the double square root,
+// then the double reciprocal, then the float conversion - for integer x in
+// [1, 2^42).  One Newton step in double from the float reciprocal square root
+// gives y within 2^-42 (relative) of 1/sqrt(x): rsqrtf is within 2 ulp
+// (2^-22) and float(x) within 2^-24, so the step's error is about
+// 1.5 * (2^-21.8)^2 plus a few double roundings.  The reference's double value
+// is within 2^-52 of 1/sqrt(x), so the two are less than 2^11 units of y's
+// last place apart, and both round to the same float unless a float rounding
+// boundary lies between them: the 29 bits below float precision of y are
+// then within 2^11 of the halfway pattern 2^28.  Whenever they are within
+// 2^16 of it (about one value in 4000) the double square root and reciprocal
+// are used instead.
+__device__ __forceinline__ float inv_sqrt_as_reference(double x) {
+    const double y = static_cast<double>(rsqrtf(__double2float_rn(x)));
+    const double y1 = __dmul_rn(y, __dsub_rn(1.5, __dmul_rn(__dmul_rn(0.5, x), __dmul_rn(y, y))));
+    const int low = static_cast<int>(static_cast<unsigned long long>(__double_as_longlong(y1)) & 0x1FFFFFFFull);
+    if (abs(low - 0x10000000) > 0x10000) return __double2float_rn(y1);
+    return __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(x)));
+}
+
 // Variance gate (face_vision_engine.cu:463-492); returns invNorm, or 0 when
 // the window is rejected.
 __device__ __forceinline__ float window_inv(const CasLevel& L, int x, int y, int winW, int winH, int normMode) {
@@ -279,7 +299,7 @@ __device__ __forceinline__ float window_inv(const CasLevel& L, int x, int y, int
     const double area = static_cast<double>(nw * nh);
     const double nf2 = __dsub_rn(__dmul_rn(area, static_cast<double>(q)), __dmul_rn(ns, ns));
     if (!(nf2 > 0.0)) return 0.0f;
-    const float inv = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(nf2)));
+    const float inv = inv_sqrt_as_reference(nf2);  // nf2: an integer in [1, 2^42)
     if (!(__dmul_rn(area, static_cast<double>(inv)) < 1e-1)) return 0.0f;
     return inv;
 }

@@ -240,55 +240,88 @@ constexpr size_t sort_smem_bytes() {
 
 // Outputs of one sorted feature (every thread of the 1024-thread CTA calls
 // this after the last pass): the split bitmask from the sorted keys (keys[]
-// in sample order, idx[] the sorted sample order; gnat is scratch for n/32
-// words), the two-copy slot assignment, and the order row, in the lane-run
-// layout when ordPadded.  idx[] is rewritten in place (slots, padding).
+// in sample order, idx[] the sorted sample order, 16-byte aligned; gnat is
+// scratch for n/16 16-bit words), the two-copy slot assignment, and the order
+// row, in the lane-run layout when ordPadded.  idx[] is rewritten in place
+// (slots, padding).
 __device__ __forceinline__ void sort_epilogue(const uint32_t* keys, uint16_t* idx, uint32_t* gnat, int n, int fl,
                                               uint16_t* __restrict__ ordOut, int64_t ordStride, bool ordPadded,
                                               uint16_t* __restrict__ gapOut, int64_t gapStride, int slotBase, int L) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int gapWords = (n + 31) >> 5;
+    const int tid = threadIdx.x;
     // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
-    // A warp takes 32 consecutive positions per step, one per lane; the
-    // next value comes from the next lane, and the word from one ballot.
-    // The words (in the free digit-counter array) are then stored in the
-    // lane-run layout of the resident orders (see ord_slot).
+    // One thread per unit of 16 consecutive positions: the unit's order
+    // entries in two 16-byte loads, all 17 values gathered before any is
+    // compared, and the unit's split bits as one 16-bit word (in the free
+    // digit-counter array); the words are then stored in the lane-run layout
+    // of the resident orders (see ord_slot; a lane run is whole units).
     if (gapOut) {
-        for (int k0 = warp * 32; k0 < gapWords * 32; k0 += kSortThreads) {
-            const int k = k0 + lane;
-            const float v0 = k < n ? __uint_as_float(radix_key_inv(keys[idx[k]])) : 0.0f;
-            float v1 = __shfl_down_sync(0xffffffffu, v0, 1);
-            if (lane == 31 && k + 1 < n) v1 = __uint_as_float(radix_key_inv(keys[idx[k + 1]]));
-            const uint32_t bits = __ballot_sync(0xffffffffu, k + 1 < n && __fadd_rn(v0, 1e-7f) < v1);
-            if (lane == 0) gnat[k0 >> 5] = bits;
+        uint16_t* gnat16 = reinterpret_cast<uint16_t*>(gnat);
+        const int units = (n + 15) >> 4;
+        for (int u = tid; u < units; u += kSortThreads) {
+            const int k0 = u * 16;
+            const uint4 a = *reinterpret_cast<const uint4*>(idx + k0);
+            const uint4 b = *reinterpret_cast<const uint4*>(idx + k0 + 8);
+            const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+            float v[17];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const uint32_t id = (w[i >> 1] >> (16 * (i & 1))) & 0xFFFFu;
+                v[i] = k0 + i < n ? __uint_as_float(radix_key_inv(keys[id])) : 0.0f;
+            }
+            v[16] = k0 + 16 < n ? __uint_as_float(radix_key_inv(keys[idx[k0 + 16]])) : 0.0f;
+            uint32_t bits = 0;
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                if (k0 + i + 1 < n && __fadd_rn(v[i], 1e-7f) < v[i + 1]) bits |= 1u << i;
+            gnat16[u] = static_cast<uint16_t>(bits);
         }
         __syncthreads();
         uint16_t* grow = gapOut + static_cast<size_t>(fl) * gapStride;
         for (int j = tid; j < 2 * L; j += kSortThreads) {
             const int k = (j & 31) * L + 16 * (j >> 5);  // first position of the word
-            grow[j] = k < n ? static_cast<uint16_t>(gnat[k >> 5] >> (k & 31)) : uint16_t(0);
+            grow[j] = k < n ? gnat16[k >> 4] : uint16_t(0);
         }
     }
     // Two weight copies: pick each position's copy.  The sweep's gather
     // instruction i of step t reads positions m*L + 16t + i, m = 0..31
-    // (lane m); one thread takes that group and assigns its members in
-    // turn to the less loaded of their two banks (greedy two-choice, loads
-    // tracked up to 2 in two bit masks: o1 = banks with load >= 1, o2 = >= 2).
+    // (lane m); thread g takes that group and assigns its members in turn to
+    // the less loaded of their two banks (greedy two-choice, bank loads
+    // tracked up to 2 in two bit masks: o1 = banks with load >= 1, o2 = banks
+    // with load 2).  The members are read eight at a time, the next eight
+    // before the current ones are decided, so no load waits on the chain of
+    // decisions.
     if (ordPadded && slotBase > 0) {
         __syncthreads();
         for (int g = tid; g < L; g += kSortThreads) {
             const int kb = 16 * (g >> 4) + (g & 15);
+            const int members = kb < n ? min(32, (n - kb + L - 1) / L) : 0;  // kb + m*L < n
+            uint32_t cur[8], nxt[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) cur[i] = i < members ? idx[kb + i * L] : 0u;
             uint32_t o1 = 0, o2 = 0;
-            for (int m = 0; m < 32 && kb + m * L < n; ++m) {
-                const uint32_t id = idx[kb + m * L];
-                const uint32_t off1 = copy1_offset(id);
-                const int b0 = id & 31, b1 = off1 & 31;
-                // copy 1 is less loaded: b0 at 1 and b1 empty, or b0 at 2 and b1 below 2
-                const bool one = ((o1 >> b0) & 1u) && !((((o2 >> b0) & 1u) ? o2 : o1) >> b1 & 1u);
-                const uint32_t bit = 1u << (one ? b1 : b0);
-                o2 |= o1 & bit;
-                o1 |= bit;
-                if (one) idx[kb + m * L] = static_cast<uint16_t>(slotBase + off1);
+#pragma unroll
+            for (int m0 = 0; m0 < 32; m0 += 8) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    nxt[i] = (m0 + 8 < 32 && m0 + 8 + i < members) ? idx[kb + (m0 + 8 + i) * L] : 0u;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int m = m0 + i;
+                    if (m < members) {
+                        const uint32_t off1 = copy1_offset(cur[i]);
+                        const int b0 = cur[i] & 31, b1 = off1 & 31;
+                        // copy 1 when its bank is strictly less loaded
+                        const uint32_t l0 = ((o1 >> b0) & 1u) + ((o2 >> b0) & 1u);
+                        const uint32_t l1 = ((o1 >> b1) & 1u) + ((o2 >> b1) & 1u);
+                        const bool one = l1 < l0;
+                        const uint32_t bit = 1u << (one ? b1 : b0);
+                        o2 |= o1 & bit;
+                        o1 |= bit;
+                        if (one) idx[kb + m * L] = static_cast<uint16_t>(slotBase + off1);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) cur[i] = nxt[i];
             }
         }
         __syncthreads();
@@ -490,13 +523,24 @@ __device__ __forceinline__ void scan_thread_counters(uint32_t* cnt, uint32_t* wa
     }
 }
 
+// Four consecutive items' sample indices (16 bits each) of a blocked pass:
+// in pass 0 the positions themselves (the sample order), later from the
+// source buffer.
+__device__ __forceinline__ uint2 load_four(const uint2* src4, int pass, int pos, int j) {
+    if (pass == 0) {
+        const uint32_t lo = static_cast<uint32_t>(pos) * 0x10001u + 0x10000u;
+        return make_uint2(lo, lo + 0x20002u);
+    }
+    return src4[j / 4];
+}
+
 template <int R, bool kFromResp>
 __global__ void __launch_bounds__(kSortThreads, 1)
 eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int featCount,
                          const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm, int n,
                          const float* __restrict__ resp, uint16_t* __restrict__ ordOut, int64_t ordStride,
                          bool ordPadded, uint16_t* __restrict__ gapOut, int64_t gapStride, int slotBase, int L) {
-    static_assert(R % 2 == 0 && R <= kBlockedMaxR, "an even number of items per thread, at most kBlockedMaxR");
+    static_assert(R % 4 == 0 && R <= kBlockedMaxR, "a multiple of 4 items per thread, at most kBlockedMaxR");
     constexpr int NP = 1024 * R;
     constexpr int kPk = (R + 5) / 6;  // words of six 5-bit digits
     extern __shared__ __align__(16) unsigned char smem[];
@@ -537,7 +581,9 @@ eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegi
         for (int pass = 0; pass < kDigitPasses; ++pass) {
             const int shift = pass * kDigitBits;
             // pass 0 takes the sample order; even passes write B, odd ones A
-            const uint32_t* src2 = reinterpret_cast<const uint32_t*>((pass & 1) ? idxB : idxA) + tid * (R / 2);
+            // a thread's R indices as R/4 8-byte words: 40 bytes apart, so a
+            // half-warp's 16 loads cover the 32 banks once
+            const uint2* src4 = reinterpret_cast<const uint2*>((pass & 1) ? idxB : idxA) + tid * (R / 4);
             uint16_t* dst = (pass & 1) ? idxA : idxB;
 #pragma unroll
             for (int c = 0; c < kCntRows; ++c) ccol[c * kCntRow] = 0;
@@ -545,11 +591,11 @@ eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegi
 #pragma unroll
             for (int c = 0; c < kPk; ++c) dg[c] = 0;
 #pragma unroll
-            for (int j = 0; j < R; j += 2) {
-                const uint32_t two = pass == 0 ? static_cast<uint32_t>(tid * R + j) * 0x10001u + 0x10000u : src2[j / 2];
+            for (int j = 0; j < R; j += 4) {
+                const uint2 four = load_four(src4, pass, tid * R + j, j);
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const uint32_t id = h ? two >> 16 : two & 0xFFFFu;
+                for (int h = 0; h < 4; ++h) {
+                    const uint32_t id = ((h < 2 ? four.x : four.y) >> (16 * (h & 1))) & 0xFFFFu;
                     const uint32_t d = (keys[id] >> shift) & 31u;
                     ccol[(d & 15u) * kCntRow] += 1u << (d & 16u);
                     dg[(j + h) / 6] |= d << (5 * ((j + h) % 6));
@@ -559,11 +605,11 @@ eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegi
             scan_thread_counters(cnt, warpTot, blockTotal);
             __syncthreads();
 #pragma unroll
-            for (int j = 0; j < R; j += 2) {
-                const uint32_t two = pass == 0 ? static_cast<uint32_t>(tid * R + j) * 0x10001u + 0x10000u : src2[j / 2];
+            for (int j = 0; j < R; j += 4) {
+                const uint2 four = load_four(src4, pass, tid * R + j, j);
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const uint32_t id = h ? two >> 16 : two & 0xFFFFu;
+                for (int h = 0; h < 4; ++h) {
+                    const uint32_t id = ((h < 2 ? four.x : four.y) >> (16 * (h & 1))) & 0xFFFFu;
                     const uint32_t d = (dg[(j + h) / 6] >> (5 * ((j + h) % 6))) & 31u;
                     uint32_t* cw = ccol + (d & 15u) * kCntRow;
                     const uint32_t w = *cw;
