@@ -46,7 +46,9 @@ struct PStumpPlanes {
 struct DStage {
     int32_t first, ntrees;
     float threshold;
-    int32_t pad;
+    // Bound on |any summation of the stage's leaf values - their exact sum|
+    // plus the same for the sequential FP32 sum (see deep_pass).
+    float tol;
 };
 
 // One pyramid level of one image, as scanned.
@@ -642,14 +644,24 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
 // ---------------------------------------------------------------------------
 // Deep pass: SL windows per warp, 32/SL lanes per window.  Each window slot
 // holds the window's (winW+1) x (winH+1) integral patch in shared memory as
-// floats; per step every slot evaluates its next 32/SL stumps (lane j of the
-// slot: stump k0 + j), the values go through a per-warp shared buffer, and
-// each slot adds its values to its stage sum in stump order, so the sum is
-// the same sequential fp32 sum as the reference's.  A slot whose window is
+// floats; per step every slot evaluates its next 32/SL stumps per lane
+// evaluation (lane j of the slot: stumps k0 + j, k0 + j + 32/SL, ...).
+//
+// A stage is decided from an order-free sum: each lane adds its own leaf
+// values, and at the end of the stage a butterfly over the slot's lanes gives
+// every lane the same total.  Any way of summing N terms, and the reference's
+// sequential FP32 sum from 0.0f, lies within the stage's `tol` of the exact
+// sum (tol >= (gamma(N-1) + gamma(N+5)) * sum of max|leaf|, gamma(k) =
+// k u / (1 - k u), u = 2^-24), so a total at or above threshold + tol passes
+// the reference's test !(acc < threshold) and one below threshold - tol fails
+// it.  A slot whose total lies in between, or that passes the last stage
+// (whose sum is the detection's score), replays the stage exactly: the values
+// go through a per-warp shared buffer and each slot adds them in stump order
+// from 0.0f, the reference's sequential FP32 sum.  A slot whose window is
 // rejected or accepted takes the next window from the queue; the whole warp
 // copies the new window's patch.
 //
-// Per-warp shared memory: 32 floats of values, then SL patches.
+// Per-warp shared memory: 32 * kDeepEvals floats of values, then SL patches.
 // ---------------------------------------------------------------------------
 constexpr int kDeepEvals = 3;  // stumps a lane evaluates per step
 __host__ __device__ constexpr int deep_warp_floats(int slots, int patchElems) {
@@ -670,7 +682,8 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
     int qi = -1;  // queue index of the slot's window, -1 = empty
     QEntry e{};
     int si = 0, k0 = 0;
-    float acc = 0.0f, score = 0.0f;
+    float acc = 0.0f, lacc = 0.0f, score = 0.0f;
+    bool exact = false;  // the slot replays its stage with the sequential sum
     bool more = true;
     for (;;) {
         // Refill empty slots one window at a time; all lanes copy the patch.
@@ -708,52 +721,88 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
                 si = P.deepFrom;
                 k0 = 0;
                 acc = 0.0f;
+                lacc = 0.0f;
+                exact = false;
                 score = ne.score;
             }
         }
         if (!__any_sync(0xffffffffu, qi >= 0)) break;
         __syncwarp();
         const bool active = qi >= 0;
-        DStage st{0, 0, 0.0f, 0};
+        DStage st{0, 0, 0.0f, 0.0f};
         if (active) st = P.stages[si];
+        float c[kDeepEvals];
 #pragma unroll
         for (int ev = 0; ev < kDeepEvals; ++ev) {
             const int k = k0 + ev * LPS + j;
-            float c = 0.0f;
-            if (active && k < st.ntrees) c = patch_stump_value(P.pstumps, st.first + k, myPatch, e.inv);
-            vals[slot * SPS + ev * LPS + j] = c;
+            c[ev] = 0.0f;
+            if (active && k < st.ntrees) c[ev] = patch_stump_value(P.pstumps, st.first + k, myPatch, e.inv);
         }
-        __syncwarp();
         const int m = active ? min(SPS, st.ntrees - k0) : 0;
-        const float4* v4 = reinterpret_cast<const float4*>(vals + slot * SPS);
+        if (__any_sync(0xffffffffu, exact)) {
 #pragma unroll
-        for (int g = 0; g < SPS / 4; ++g) {
-            const float4 x = v4[g];
-            if (4 * g + 0 < m) acc = __fadd_rn(acc, x.x);
-            if (4 * g + 1 < m) acc = __fadd_rn(acc, x.y);
-            if (4 * g + 2 < m) acc = __fadd_rn(acc, x.z);
-            if (4 * g + 3 < m) acc = __fadd_rn(acc, x.w);
+            for (int ev = 0; ev < kDeepEvals; ++ev) vals[slot * SPS + ev * LPS + j] = c[ev];
+            __syncwarp();
+            if (exact) {
+                const float4* v4 = reinterpret_cast<const float4*>(vals + slot * SPS);
+#pragma unroll
+                for (int g = 0; g < SPS / 4; ++g) {
+                    const float4 x = v4[g];
+                    if (4 * g + 0 < m) acc = __fadd_rn(acc, x.x);
+                    if (4 * g + 1 < m) acc = __fadd_rn(acc, x.y);
+                    if (4 * g + 2 < m) acc = __fadd_rn(acc, x.z);
+                    if (4 * g + 3 < m) acc = __fadd_rn(acc, x.w);
+                }
+            }
+            __syncwarp();
         }
-        __syncwarp();
+        if (!exact) {
+#pragma unroll
+            for (int ev = 0; ev < kDeepEvals; ++ev) lacc = __fadd_rn(lacc, c[ev]);
+        }
         if (j == 0) evals += static_cast<unsigned>(m);
         k0 += SPS;
-        if (active && k0 >= st.ntrees) {
-            if (acc < st.threshold) {
-                qi = -1;
-            } else {
-                score = acc;
-                ++si;
+        const bool done = active && k0 >= st.ntrees;
+        float tot = lacc;
+        if (__any_sync(0xffffffffu, done && !exact)) {
+#pragma unroll
+            for (int o = LPS / 2; o > 0; o >>= 1) tot = __fadd_rn(tot, __shfl_xor_sync(0xffffffffu, tot, o));
+        }
+        if (done) {
+            // 1 pass, 0 reject, -1 replay the stage exactly
+            int verdict;
+            if (exact)
+                verdict = acc < st.threshold ? 0 : 1;
+            else if (tot < __fsub_rd(st.threshold, st.tol))
+                verdict = 0;
+            else if (tot >= __fadd_ru(st.threshold, st.tol) && si + 1 < P.nStages)
+                verdict = 1;
+            else
+                verdict = -1;
+            if (verdict < 0) {
+                exact = true;
                 k0 = 0;
                 acc = 0.0f;
-                if (si >= P.nStages) {
-                    if (j == 0) {
-                        const CasLevel& L = P.levels[e.level];
-                        const int slotOut = atomicAdd(P.counts + L.image, 1);
-                        if (slotOut < P.detCap)
-                            P.dets[static_cast<size_t>(L.image) * P.detCap + slotOut] =
-                                make_detection(L, e, P.winW, P.winH, score);
-                    }
+            } else {
+                exact = false;
+                lacc = 0.0f;
+                if (verdict == 0) {
                     qi = -1;
+                } else {
+                    score = acc;  // exact on the last stage, which is always replayed
+                    ++si;
+                    k0 = 0;
+                    acc = 0.0f;
+                    if (si >= P.nStages) {
+                        if (j == 0) {
+                            const CasLevel& L = P.levels[e.level];
+                            const int slotOut = atomicAdd(P.counts + L.image, 1);
+                            if (slotOut < P.detCap)
+                                P.dets[static_cast<size_t>(L.image) * P.detCap + slotOut] =
+                                    make_detection(L, e, P.winW, P.winH, score);
+                        }
+                        qi = -1;
+                    }
                 }
             }
         }

@@ -930,7 +930,20 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
         if (stages[i].ntrees < 0 || stages[i].first < 0 ||
             static_cast<int64_t>(stages[i].first) + stages[i].ntrees > stumpCount)
             return set_error(VJ_INVALID_ARG, "vj_detector_set_model: stage outside the stump array");
-        dst[static_cast<size_t>(i)] = DStage{stages[i].first, stages[i].ntrees, stages[i].threshold, 0};
+        // tolerance of the deep pass's order-free stage sums (cascade.cuh deep_pass)
+        double lim = 0.0;
+        for (int k = 0; k < stages[i].ntrees; ++k) {
+            const vj_stump4& sk = stumps[stages[i].first + k];
+            lim += std::max(std::fabs(static_cast<double>(sk.leftVal)), std::fabs(static_cast<double>(sk.rightVal)));
+        }
+        const double u = std::ldexp(1.0, -24), nt = stages[i].ntrees;
+        auto gamma = [&](double k) { return k * u / (1.0 - k * u); };
+        // relative rounding of both sums, plus half an ulp of the smallest
+        // subnormal per operation, rounded up to a float
+        const double bound = 1.01 * (gamma(nt - 1.0 > 0.0 ? nt - 1.0 : 0.0) + gamma(nt + 5.0)) * lim +
+                             (2.0 * nt + 6.0) * std::ldexp(1.0, -150);
+        const float tol = std::nextafter(static_cast<float>(bound), INFINITY);
+        dst[static_cast<size_t>(i)] = DStage{stages[i].first, stages[i].ntrees, stages[i].threshold, tol};
     }
     int st;
     if ((st = d->stumps.ensure(sizeof(DStump) * ds.size())) != VJ_OK) return st;

@@ -152,3 +152,72 @@ def test_barrier_wait_runs_out_and_context_survives(cuda, vj, basic_pool, full_c
     assert lib.vj_detector_test_barrier_timeout(e._h, -1, 0) == 0
     s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
     assert s == 0 and raw.tobytes() == ref.tobytes()
+
+
+def _stage_sums(pool, st, sg, scene, oracle, last):
+    """The reference's FP32 stage sums (stumps added in order from 0.0f) of
+    every full-size window of the image, stages 0..last, with the survivors of
+    each stage; restated from detectMultiScaleCpu (src/main.cu:755-819) on the
+    first pyramid level (the image itself, step 1)."""
+    s, q = oracle.integral(scene)
+    S = s.astype(np.int64).ravel()
+    Q = q.astype(np.uint64).ravel()
+    h, w = scene.shape
+    P = w + 1
+    ys, xs = np.mgrid[0:h - 23, 0:w - 23]
+    b = (ys * P + xs).ravel()
+    o = [P + 1, P + 23, 23 * P + 1, 23 * P + 23]
+    ns = (S[b + o[0]] - S[b + o[1]] - S[b + o[2]] + S[b + o[3]]).astype(np.float64)
+    m32 = np.uint64(0xFFFFFFFF)
+    qq = ((Q[b + o[0]] - Q[b + o[1]] - Q[b + o[2]] + Q[b + o[3]]) & m32).astype(np.float64)
+    nf2 = 484.0 * qq - ns * ns
+    inv = np.zeros(len(b), np.float32)
+    pos = nf2 > 0
+    inv[pos] = (1.0 / np.sqrt(nf2[pos])).astype(np.float32)
+    alive = np.nonzero(pos & (484.0 * inv.astype(np.float64) < 0.1))[0]
+    fidx = st["featureBits"].view(np.int32)
+    out = []
+    for k in range(last + 1):
+        f0, nt, thr = int(sg[k]["first"]), int(sg[k]["ntrees"]), np.float32(sg[k]["threshold"])
+        bb = b[alive]
+        acc = np.zeros(len(alive), np.float32)
+        for j in range(nt):
+            ft = pool[fidx[f0 + j]]
+            raw = np.zeros(len(alive), np.float32)
+            for ri, r in enumerate(("r0", "r1", "r2")[:int(ft["rectCount"])]):
+                c = [S[bb + (int(ft[r][p]) // 25) * P + int(ft[r][p]) % 25].astype(np.float32)
+                     for p in ("p0", "p1", "p2", "p3")]
+                v = (((c[0] - c[1]) - c[2]) + c[3]) * np.float32(ft[r]["w"])
+                raw = v if ri == 0 else (raw + v)
+            resp = raw * inv[alive]
+            acc = acc + np.where(resp < st["theta"][f0 + j], st["leftVal"][f0 + j], st["rightVal"][f0 + j])
+        out.append((alive.copy(), acc))
+        alive = alive[~(acc < thr)]
+    return out
+
+
+def test_deep_stage_sums_on_the_threshold(cuda, vj, oracle, basic_pool):
+    """Deep-pass stages decide from order-free sums and replay a stage with the
+    sequential FP32 sum when the total is within the stage's tolerance of its
+    threshold.  Thresholds placed exactly on a window's sequential sum (which
+    passes: !(acc < threshold)) and one ulp above another window's sum (which
+    fails) must give the oracle's detections."""
+    st, sg = vj.synth_cascade(2)
+    sg = sg.copy()
+    scene = vj.synth_scene(21, 160, 120, 2, 24, 60)
+    e = engine(vj, basic_pool, st, sg)
+    deep_from = 4  # stages 0-3 run in the tile pass with the default config
+    for k in (deep_from, deep_from + 1, deep_from + 2):
+        sums = _stage_sums(basic_pool, st, sg, scene, oracle, k)
+        alive, acc = sums[k]
+        assert len(alive) > 4, k
+        order = np.argsort(acc)
+        pick = acc[order[len(order) // 3]]
+        # every survivor at or above `pick` passes, the ones below fail
+        sg[k]["threshold"] = pick if k != deep_from + 1 else np.nextafter(pick, np.float32(np.inf))
+    ref = oracle.detect(basic_pool, st, sg, scene, norm_mode=0, threads=8)
+    e = engine(vj, basic_pool, st, sg)
+    h, w = scene.shape
+    s, raw = e.detectMultiScale(scene, w, h, w, 1.25, 4, 24, 200000, applyGrouping=False)
+    assert s == 0
+    assert len(raw) == len(ref) and raw.tobytes() == ref.tobytes()
