@@ -384,11 +384,12 @@ def run_gpu(args, rank, world):
     # DRAM bytes (read + write) per feature-sample of one launch, from ncu's
     # dram__bytes counters on the 16,384-feature x 20,000-sample case, scaled
     # to this launch's size.
-    traffic_per_unit = {"sweep_kernel": (713.146368e6 + 3.349760e6) / (16384 * 20000),
-                        "eval_sort_kernel": (230.055936e6 + 669.191168e6) / (16384 * 20000)}
+    traffic_per_unit = {"sweep_kernel": (713.394432e6 + 3.844096e6) / (16384 * 20000),
+                        "eval_sort_kernel": (212.687104e6 + 666.141184e6) / (16384 * 20000)}
     notes = {"sweep_kernel": "streams the resident orders once per round; HBM is its roofline",
-             "eval_sort_kernel": "once per stage; an on-chip sort bound by the ALU pipe (stable ballot "
-                                 "ranking), its HBM fraction is informational"}
+             "eval_sort_kernel": "once per stage; an on-chip radix sort bound by the shared-memory pipe "
+                                 "(per-thread digit counters, random key gathers and index scatters), its "
+                                 "HBM fraction is informational"}
 
     def roofline_of(name):
         launches, total = prof[name]

@@ -206,7 +206,7 @@ def test_deep_stage_sums_on_the_threshold(cuda, vj, oracle, basic_pool):
     sg = sg.copy()
     scene = vj.synth_scene(21, 160, 120, 2, 24, 60)
     e = engine(vj, basic_pool, st, sg)
-    deep_from = 4  # stages 0-3 run in the tile pass with the default config
+    deep_from = 5  # stages 0-4 (111 stumps) run in the tile pass with the default config
     for k in (deep_from, deep_from + 1, deep_from + 2):
         sums = _stage_sums(basic_pool, st, sg, scene, oracle, k)
         alive, acc = sums[k]
