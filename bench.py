@@ -391,6 +391,15 @@ def run_gpu(args, rank, world):
                                  "(per-thread digit counters, random key gathers and index scatters), its "
                                  "HBM fraction is informational"}
 
+    # The sort is bound by the shared-memory pipe, not by HBM: its wavefronts per
+    # feature-sample from ncu's l1tex__data_pipe_lsu_wavefronts_mem_shared.sum on
+    # the same 16,384 x 20,000 case, against one wavefront per cycle per SM at the
+    # SM clock sampled during the timed steps (a nominal figure, not a measured peak).
+    smem_wavefronts_per_unit = {"eval_sort_kernel": 1237173413 / (16384 * 20000)}
+    clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
     def roofline_of(name):
         launches, total = prof[name]
         avg_ms = total / max(1, launches)
@@ -405,6 +414,14 @@ def run_gpu(args, rank, world):
             r.update({"achieved": ach, "frac": ach / peak, "algorithmic_bytes_per_launch": kbytes[name]})
         if name in notes:
             r["note"] = notes[name]
+        if name in smem_wavefronts_per_unit and avg_ms > 0:
+            ach = smem_wavefronts_per_unit[name] * units_per_launch[name] / (avg_ms * 1e-3)
+            pk = sms * sm_mhz * 1e6
+            r["onchip"] = {"bound": "shared-memory pipe", "unit": "wavefronts/s", "achieved": ach, "peak": pk,
+                           "peak_kind": "nominal: 1 wavefront per cycle per SM at the sampled SM clock",
+                           "frac": ach / pk,
+                           "source": "ncu l1tex__data_pipe_lsu_wavefronts_mem_shared.sum at 16,384 features x "
+                                     "20,000 samples, scaled by features x samples"}
         return r
 
     dom = max(prof.items(), key=lambda kv: kv[1][1])[0] if prof else None
@@ -431,7 +448,7 @@ def run_gpu(args, rank, world):
                           "streamed_fraction": swept_per_launch / F_local if F_local else None,
                           "note": "from the second round of a stage, features whose error bound cannot reach the "
                                   "candidate window are not streamed; picks are unchanged"},
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "picks_head": [int(x) for x in weaks["featureIdx"][:5]],
     }
     if rank == 0 and world == 1:
