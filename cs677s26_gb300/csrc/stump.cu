@@ -1086,6 +1086,13 @@ __global__ void select_candidates_kernel(const float* __restrict__ fastErr, int 
 //    with the CPU's update rule (lower err wins; at equal err parity +1
 //    replaces parity -1).
 // ---------------------------------------------------------------------------
+constexpr int kRefinePairs = kRefineWarps / 2;  // candidates a block takes at once
+
+// Named barrier of the two warps of pair `pair` (barrier 0 is __syncthreads).
+__device__ __forceinline__ void pair_sync(int pair) {
+    asm volatile("bar.sync %0, 64;" ::"r"(pair + 1) : "memory");
+}
+
 template <bool kSmemW>
 __global__ void __launch_bounds__(kRefineThreads)
 refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t* __restrict__ gap,
@@ -1095,11 +1102,14 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
               unsigned long long* __restrict__ candKey, float2* __restrict__ prefix, int64_t prefixStride,
               const int* gate) {
     if (gate_closed(gate)) return;
-    if (static_cast<int>(blockIdx.x) * kRefineWarps >= prm->ncand) return;  // no candidate in this block
+    if (static_cast<int>(blockIdx.x) * kRefinePairs >= prm->ncand) return;  // no candidate in this block
     extern __shared__ float wsgS[];
-    // per warp and chunk position: first the (positive, negative) addends of
-    // the position's sample, then, in place, the left sums after it
-    __shared__ __align__(16) float2 pre[kRefineWarps][256];
+    // per pair, two chunk buffers of 256 positions: first the (positive,
+    // negative) addends of each position's sample, then, in place, the left
+    // sums after it
+    __shared__ __align__(16) float2 pre[kRefinePairs][2][256];
+    __shared__ float2 totals[kRefinePairs];
+    __shared__ unsigned long long pairBest[kRefinePairs];
     const float* wsg = wsgG;
     if (kSmemW) {
         fill_weights(wsgS, wsgG, n, slotBase);
@@ -1107,28 +1117,35 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
         wsg = wsgS;
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kRefineWarps + w;  // row of `prefix` this warp uses
+    const int pr = w >> 1;          // the pair of warps this warp belongs to
+    const bool chainer = (w & 1);   // second warp of the pair: runs the chains
+    const int gw = blockIdx.x * kRefineWarps + 2 * pr;  // row of `prefix` the pair uses
     const int nc = prm->ncand;
-    // One warp per candidate feature.  The warp streams the feature's sorted
-    // order 256 positions at a time (one coalesced 16-byte load per lane,
-    // issued a chunk ahead), gathers the signed weights and stores each
+    const int chunks = (n + 255) / 256;
+    // Two warps per candidate feature.  The first streams the feature's
+    // sorted order 256 positions at a time (one coalesced 16-byte load per
+    // lane, issued a chunk ahead), gathers the signed weights and stores each
     // position's two addends (|w| to its class's sum, +0.0f to the other) in
-    // order, and lane 0 replays the reference's sequential FP32 additions
-    // (main.cu:626-678) from there.  Inactive samples carry a zero weight and
-    // the accumulator of the other class adds +0.0f: both leave an FP32 sum
-    // of non-negative terms unchanged, exactly as skipping them does.
-    for (int c = blockIdx.x * kRefineWarps + w; c < nc; c += gridDim.x * kRefineWarps) {
+    // order into one of the pair's two chunk buffers, while lane 0 of the
+    // second warp replays the reference's sequential FP32 additions
+    // (main.cu:626-678) over the previous chunk in the other buffer and the
+    // second warp copies that chunk's left sums to the pair's row of
+    // `prefix`.  Inactive samples carry a zero weight and the accumulator of
+    // the other class adds +0.0f: both leave an FP32 sum of non-negative
+    // terms unchanged, exactly as skipping them does.
+    for (int c = blockIdx.x * kRefinePairs + pr; c < nc; c += gridDim.x * kRefinePairs) {
         const int f = cand[c];
         const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
         const uint16_t* grow = gap + static_cast<size_t>(f) * gapStride;
+        float2* prow = prefix + static_cast<size_t>(gw) * prefixStride;
         auto load = [&](int base) {
             const int k0 = base + lane * 8;
             return (k0 < n) ? __ldg(reinterpret_cast<const uint4*>(row + ord_slot(k0, L))) : make_uint4(0, 0, 0, 0);
         };
-        auto gather = [&](int base, const uint4& v) {
+        auto gather = [&](int base, const uint4& v, float2* buf) {
             const int k0 = base + lane * 8;
             const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-            float4* st = reinterpret_cast<float4*>(&pre[w][lane * 8]);
+            float4* st = reinterpret_cast<float4*>(buf + lane * 8);
 #pragma unroll
             for (int h = 0; h < 8; h += 2) {
                 float ap[2], an[2];
@@ -1144,46 +1161,57 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
                 st[h >> 1] = make_float4(ap[0], an[0], ap[1], an[1]);
             }
         };
-        // One sequential pass (lane 0): the left sums after every position, in
-        // sorted order, into the warp's row of `prefix`.  Carried on to the last
-        // position, the same chain gives the totals: the reference adds the
-        // same weights in the same order for both (main.cu:626-645).
-        float2* prow = prefix + static_cast<size_t>(gw) * prefixStride;
+        // One sequential pass: the left sums after every position, in sorted
+        // order.  Carried on to the last position, the same chain gives the
+        // totals: the reference adds the same weights in the same order for
+        // both (main.cu:626-645).  Step i: the gatherer fills chunk i's buffer
+        // while the chainer sums chunk i - 1.
         float tp = 0.0f, tn = 0.0f;
-        {
-            uint4 v = load(0);
-            for (int base = 0; base < n; base += 256) {
-                const uint4 vn = load(base + 256);
-                gather(base, v);
-                __syncwarp();
+        uint4 v = chainer ? make_uint4(0, 0, 0, 0) : load(0);
+        for (int i = 0; i <= chunks; ++i) {
+            if (!chainer) {
+                if (i < chunks) {
+                    const uint4 vn = load((i + 1) * 256);
+                    gather(i * 256, v, pre[pr][i & 1]);
+                    v = vn;
+                }
+            } else if (i > 0) {
+                const int base = (i - 1) * 256;
+                float2* buf = pre[pr][(i - 1) & 1];
                 if (lane == 0) {
-                    float4* st = reinterpret_cast<float4*>(pre[w]);
-#pragma unroll 8
-                    for (int j = 0; j < 128; ++j) {
-                        const float4 q = st[j];
-                        const float p0 = __fadd_rn(tp, q.x), n0 = __fadd_rn(tn, q.y);
-                        tp = __fadd_rn(p0, q.z);
-                        tn = __fadd_rn(n0, q.w);
-                        st[j] = make_float4(p0, n0, tp, tn);
+                    float4* st = reinterpret_cast<float4*>(buf);
+                    for (int j0 = 0; j0 < 128; j0 += 8) {
+                        float4 q[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) q[j] = st[j0 + j];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const float p0 = __fadd_rn(tp, q[j].x), n0 = __fadd_rn(tn, q[j].y);
+                            tp = __fadd_rn(p0, q[j].z);
+                            tn = __fadd_rn(n0, q[j].w);
+                            q[j] = make_float4(p0, n0, tp, tn);
+                        }
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) st[j0 + j] = q[j];
                     }
                 }
                 __syncwarp();
-                // the chunk's left sums to the warp's row, all lanes, coalesced
+                // the chunk's left sums to the pair's row, coalesced
                 const int lim = min(256, n - 1 - base);  // positions scored: 0 .. n-2
-                for (int q = lane; q < lim; q += 32) prow[base + q] = pre[w][q];
-                __syncwarp();
-                v = vn;
+                for (int q = lane; q < lim; q += 32) prow[base + q] = buf[q];
             }
+            pair_sync(pr);
         }
-        tp = __shfl_sync(0xffffffffu, tp, 0);
-        tn = __shfl_sync(0xffffffffu, tn, 0);
-        __syncwarp();
-        // Scoring, every lane over its positions.  The reference's update rule
-        // over the candidates in split order (lower error replaces; at equal
-        // error parity +1 replaces parity -1) picks the lexicographic minimum
-        // of (error, parity +1 before -1, split index); errors are >= +0, so
-        // the float bits order like the values and the triple packs into one
-        // key.
+        if (chainer && lane == 0) totals[pr] = make_float2(tp, tn);
+        pair_sync(pr);
+        tp = totals[pr].x;
+        tn = totals[pr].y;
+        // Scoring, both warps, chunks alternating between them, every lane
+        // over its positions.  The reference's update rule over the
+        // candidates in split order (lower error replaces; at equal error
+        // parity +1 replaces parity -1) picks the lexicographic minimum of
+        // (error, parity +1 before -1, split index); errors are >= +0, so the
+        // float bits order like the values and the triple packs into one key.
         unsigned long long best = ~0ull;
         // the 8 split bits of positions k0..k0+7 (one lane run, one bitmask
         // word) and the left sums at the valid ones; issued a chunk ahead
@@ -1198,11 +1226,12 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
             for (int h = 0; h < 8; ++h) lv[h] = ((g >> h) & 1u) ? prow[k0 + h] : make_float2(0.0f, 0.0f);
             return g;
         };
+        const int first = chainer ? 256 : 0;
         float2 lc[8];
-        uint32_t gc = sload(0, lc);
-        for (int base = 0; base < n - 1; base += 256) {
+        uint32_t gc = sload(first, lc);
+        for (int base = first; base < n - 1; base += 512) {
             float2 ln[8];
-            const uint32_t gn = sload(base + 256, ln);
+            const uint32_t gn = sload(base + 512, ln);
             const int k0 = base + lane * 8;
 #pragma unroll
             for (int h = 0; h < 8; ++h) {
@@ -1223,7 +1252,10 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-        if (lane == 0) {
+        if (chainer && lane == 0) pairBest[pr] = best;
+        pair_sync(pr);
+        if (!chainer && lane == 0) {
+            best = min(best, pairBest[pr]);
             // (error bits, featureIdx) of every candidate, for the runner-up report
             candKey[c] = best != ~0ull ? (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f) : ~0ull;
             if (best != ~0ull) {
@@ -1232,6 +1264,8 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
                 atomicMin(&prm->winner, (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f));
             }
         }
+        // the pair's buffers, totals and best are reused by its next candidate
+        pair_sync(pr);
     }
 }
 
