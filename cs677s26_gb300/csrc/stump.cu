@@ -1464,6 +1464,220 @@ refine_shared_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const 
     }
 }
 
+// The replay with the two class chains decoupled, for n <= kRefineSplitMaxN:
+// one candidate per CTA.  In a candidate's sorted order the classes come in
+// long runs (a good feature separates them), so per-chunk class lists leave
+// one chain idle most of the time.  Here the whole order is split first:
+//   A. all warps gather every chunk (the sample of each position - its slot
+//      mapped back - and its signed weight), keep |w| per position and a
+//      bitmask of the positive positions, and count each chunk's positives;
+//   B. an exclusive scan of the chunk counts places every position in one of
+//      two in-order lists, positives from 0 and negatives from negOff;
+//   C. lane 0 of warp 0 adds the positive list and lane 1 the negative list
+//      in place, the reference's two sequential FP32 sums (main.cu:626-645),
+//      concurrently, 4 addends per 16-byte load, the next load issued ahead;
+//      the shorter chain adds +0.0f past its end (no change);
+//   D. every position's left sums are its class lists' running sums at its
+//      inclusive class ranks, read directly while scoring.
+// Inactive samples (+-0 weights) add +0.0f to their class's chain, which
+// leaves it unchanged, as in the reference's totals.
+constexpr int kRefineSplitMaxN = 26112;  // 8.125 B per position + 64 B of dynamic shared memory
+
+template <bool kTwoCopy>
+__global__ void __launch_bounds__(kRefineThreads)
+refine_split_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t* __restrict__ gap,
+                    int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, int L,
+                    RoundParams* __restrict__ prm, const int* __restrict__ cand, int8_t* __restrict__ refParity,
+                    int* __restrict__ refSplit, unsigned long long* __restrict__ candKey, const int* gate) {
+    if (gate_closed(gate)) return;
+    const int nc = prm->ncand;
+    if (static_cast<int>(blockIdx.x) >= nc) return;
+    const int chunks = (n + 255) / 256, nv = chunks * 256;
+    extern __shared__ __align__(16) float rsm[];
+    float* val = rsm;                                               // [nv] |w| per position
+    float* lists = rsm + nv;                                        // [nv + 16] the two class lists
+    uint32_t* posMask = reinterpret_cast<uint32_t*>(lists + nv + 16);  // [nv / 32]
+    constexpr int kMaxChunks = (kRefineSplitMaxN + 255) / 256;
+    __shared__ int chunkPos[kMaxChunks];  // positives before each chunk
+    __shared__ int totP, negOff;
+    __shared__ unsigned long long warpBest[kRefineWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = blockIdx.x; c < nc; c += gridDim.x) {
+        const int f = cand[c];
+        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
+        const uint16_t* grow = gap + static_cast<size_t>(f) * gapStride;
+        // A. gather
+        for (int i = w; i < chunks; i += kRefineWarps) {
+            const int k0 = i * 256 + lane * 8;
+            const uint4 v =
+                k0 < n ? __ldg(reinterpret_cast<const uint4*>(row + ord_slot(k0, L))) : make_uint4(0, 0, 0, 0);
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+            float e[8];
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                uint32_t id = (w4[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
+                if (kTwoCopy) id = slot_sample(id, slotBase);
+                e[h] = k0 + h < n ? __ldg(wsgG + id) : 0.0f;
+            }
+            uint32_t pm = 0;
+#pragma unroll
+            for (int h = 0; h < 8; ++h)
+                if (k0 + h < n && !signbit(e[h])) pm |= 1u << h;
+            reinterpret_cast<float4*>(val + k0)[0] = make_float4(fabsf(e[0]), fabsf(e[1]), fabsf(e[2]), fabsf(e[3]));
+            reinterpret_cast<float4*>(val + k0)[1] = make_float4(fabsf(e[4]), fabsf(e[5]), fabsf(e[6]), fabsf(e[7]));
+            // four lanes' 8-bit masks make one word
+            uint32_t word = pm;
+            word |= __shfl_down_sync(0xffffffffu, pm, 1) << 8;
+            word |= __shfl_down_sync(0xffffffffu, pm, 2) << 16;
+            word |= __shfl_down_sync(0xffffffffu, pm, 3) << 24;
+            if ((lane & 3) == 0) posMask[i * 8 + (lane >> 2)] = word;
+            const int cnt = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(__popc(pm)));
+            if (lane == 0) chunkPos[i] = cnt;
+        }
+        __syncthreads();
+        // B. chunk offsets (warp 0), then the two lists
+        if (w == 0) {
+            int carry = 0;
+            for (int i0 = 0; i0 < chunks; i0 += 32) {
+                const int x = i0 + lane < chunks ? chunkPos[i0 + lane] : 0;
+                int incl = x;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (i0 + lane < chunks) chunkPos[i0 + lane] = carry + incl - x;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            if (lane == 0) {
+                totP = carry;
+                negOff = (carry + 3) & ~3;
+            }
+        }
+        __syncthreads();
+        const int P = totP, N = n - P, nOff = negOff;
+        for (int i = w; i < chunks; i += kRefineWarps) {
+            const int k0 = i * 256 + lane * 8;
+            const uint32_t pm = (posMask[i * 8 + (lane >> 2)] >> (8 * (lane & 3))) & 0xFFu;
+            const int mine = __popc(pm);
+            int before = mine;  // positives of the chunk before this lane's positions
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, before, o);
+                if (lane >= o) before += y;
+            }
+            before -= mine;
+            int rp = chunkPos[i] + before;                        // rank of the next positive
+            int rn = (i * 256 - chunkPos[i]) + (lane * 8 - before);  // of the next negative
+            const float4 a = reinterpret_cast<const float4*>(val + k0)[0];
+            const float4 b = reinterpret_cast<const float4*>(val + k0)[1];
+            const float x8[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                if (k0 + h < n) {
+                    if ((pm >> h) & 1u)
+                        lists[rp++] = x8[h];
+                    else
+                        lists[nOff + rn++] = x8[h];
+                }
+            }
+        }
+        __syncthreads();
+        // C. the two chains, concurrently
+        if (w == 0 && lane < 2) {
+            const int base = lane == 0 ? 0 : nOff;
+            const int mine = lane == 0 ? P : N;
+            const int m4 = (max(P, N) + 3) & ~3;
+            const int last4 = mine > 0 ? ((mine - 1) & ~3) : 0;  // loads stay within the own list
+            float t = 0.0f;
+            auto ld = [&](int j) {
+                float4 q = *reinterpret_cast<const float4*>(lists + base + min(j, last4));
+                if (j + 0 >= mine) q.x = 0.0f;
+                if (j + 1 >= mine) q.y = 0.0f;
+                if (j + 2 >= mine) q.z = 0.0f;
+                if (j + 3 >= mine) q.w = 0.0f;
+                return q;
+            };
+            float4 q0 = ld(0), q1 = ld(4);
+            for (int j = 0; j < m4; j += 4) {
+                const float4 q2 = ld(j + 8);
+                float4 r;
+                t = __fadd_rn(t, q0.x);
+                r.x = t;
+                t = __fadd_rn(t, q0.y);
+                r.y = t;
+                t = __fadd_rn(t, q0.z);
+                r.z = t;
+                t = __fadd_rn(t, q0.w);
+                r.w = t;
+                if (j < mine) *reinterpret_cast<float4*>(lists + base + j) = r;
+                q0 = q1;
+                q1 = q2;
+            }
+        }
+        __syncthreads();
+        const float TP = P > 0 ? lists[P - 1] : 0.0f;
+        const float TN = N > 0 ? lists[nOff + N - 1] : 0.0f;
+        // D. scoring: the reference's update rule over the splits in order
+        // (lower error replaces; at equal error parity +1 replaces parity -1)
+        // picks the lexicographic minimum of (error, parity +1 before -1, split
+        // index); errors are >= +0, so the float bits order like the values
+        // and the triple packs into one key.  A position's left sums are the
+        // running sums at its inclusive class ranks.
+        unsigned long long best = ~0ull;
+        for (int i = w; i < chunks; i += kRefineWarps) {
+            const int k0 = i * 256 + lane * 8;
+            const uint32_t pm = (posMask[i * 8 + (lane >> 2)] >> (8 * (lane & 3))) & 0xFFu;
+            const int mine = __popc(pm);
+            int before = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, before, o);
+                if (lane >= o) before += y;
+            }
+            before -= mine;
+            if (k0 >= n - 1) continue;
+            const int l = k0 / L, r = k0 - l * L;
+            const uint32_t g = (static_cast<uint32_t>(__ldg(grow + (r >> 4) * 32 + l)) >> (r & 15)) & 0xFFu;  // gap_word
+            int cp = chunkPos[i] + before, cn = (i * 256 - chunkPos[i]) + (lane * 8 - before);
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                if ((pm >> h) & 1u)
+                    ++cp;
+                else
+                    ++cn;
+                if ((g >> h) & 1u) {
+                    const float lp = cp > 0 ? lists[cp - 1] : 0.0f;
+                    const float ln = cn > 0 ? lists[nOff + cn - 1] : 0.0f;
+                    const float eL = __fadd_rn(ln, __fsub_rn(TP, lp));  // parity -1
+                    const float eR = __fadd_rn(lp, __fsub_rn(TN, ln));  // parity +1
+                    const unsigned kk = static_cast<unsigned>(k0 + h);
+                    const unsigned long long kL =
+                        (static_cast<unsigned long long>(__float_as_uint(eL)) << 32) | 0x80000000u | kk;
+                    const unsigned long long kR = (static_cast<unsigned long long>(__float_as_uint(eR)) << 32) | kk;
+                    best = min(best, min(kL, kR));
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+        if (lane == 0) warpBest[w] = best;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < kRefineWarps; ++k) best = min(best, warpBest[k]);
+            // (error bits, featureIdx) of every candidate, for the runner-up report
+            candKey[c] = best != ~0ull ? (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f) : ~0ull;
+            if (best != ~0ull) {
+                refParity[f] = (best & 0x80000000ull) ? int8_t(-1) : int8_t(1);
+                refSplit[f] = static_cast<int>(best & 0x7FFFFFFFull);
+                atomicMin(&prm->winner, (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f));
+            }
+        }
+        // the lists and masks are reused by the CTA's next candidate
+        __syncthreads();
+    }
+}
+
 // 5. Winner -> TileBestCandidate with theta = 0.5f * (v[k] + v[k+1]).
 // feats and the candidate indices are relative to the searched range, which
 // starts at featBase of the pool; the output featureIdx is the pool's.
@@ -2356,7 +2570,17 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
                     select_candidates_kernel<<<std::min(div_up(F, 256), 4 * sm_count()), 256, 0, s>>>(
                         t->d_fastErr, F, t->d_prm, t->d_cand, t->d_gate));
     VJ_LAUNCH_CHECK("select_candidates_kernel");
-    if (n <= kRefineSharedMaxN) {
+    if (n <= kRefineSplitMaxN) {
+        auto k = sb > 0 ? refine_split_kernel<true> : refine_split_kernel<false>;
+        const size_t nv = static_cast<size_t>((n + 255) / 256) * 256;
+        const size_t lbytes = sizeof(float) * (2 * nv + 16) + sizeof(uint32_t) * (nv / 32);
+        VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lbytes)));
+        VJ_TIMED_LAUNCH("refine_kernel", s,
+                        k<<<refine_blocks(), kRefineThreads, lbytes, s>>>(
+                            t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb, t->laneRun, t->d_prm,
+                            t->d_cand, t->d_refParity, t->d_refSplit, t->d_candKey, t->d_gate));
+        VJ_LAUNCH_CHECK("refine_split_kernel");
+    } else if (n <= kRefineSharedMaxN) {
         auto k = sb > 0 ? refine_shared_kernel<true> : refine_shared_kernel<false>;
         const size_t lbytes = sizeof(float2) * static_cast<size_t>(n);
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lbytes)));
