@@ -1269,201 +1269,6 @@ refine_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_
     }
 }
 
-// The same replay with every left sum of the candidate in shared memory, for
-// n <= kRefineSharedMaxN: one candidate per CTA (8 warps).  Chunks of 256
-// sorted positions go through the CTA in sets of kRefineGatherWarps: in step
-// k warps 0..6 each gather one chunk of set k (the sample of every position -
-// the slot mapped back to its sample - and its signed weight from global
-// memory) and split it by class into two in-order lists of addends with each
-// position's inclusive counts of both classes, while warp 7 runs set k - 1:
-// lane 0 adds the positive list and lane 1 the negative list to their
-// sequential FP32 sums (the two chains of the reference, main.cu:626-645,
-// now each as long as its class), then the warp expands the running sums to
-// every position's left sums in shared memory.  A position of the other class
-// adds nothing to a chain, as +0.0f did; inactive samples (+-0 weights) add
-// +0.0f to their class's chain, which leaves it unchanged.  The scoring then
-// reads the left sums from shared memory with all 8 warps.
-constexpr int kRefineGatherWarps = 7;
-constexpr int kRefineSharedMaxN = 22528;  // 8 B of left sums per position in dynamic shared memory
-
-struct RefChunk {
-    float pos[256];     // addends of the positive class in sorted order, then their running sums
-    float neg[256];
-    uint32_t cnt[256];  // per position: inclusive count of positives << 16 | of negatives
-    int np, nn;
-};
-
-template <bool kTwoCopy>
-__global__ void __launch_bounds__(kRefineThreads)
-refine_shared_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t* __restrict__ gap,
-                     int64_t gapStride, const float* __restrict__ wsgG, int n, int slotBase, int L,
-                     RoundParams* __restrict__ prm, const int* __restrict__ cand, int8_t* __restrict__ refParity,
-                     int* __restrict__ refSplit, unsigned long long* __restrict__ candKey, const int* gate) {
-    if (gate_closed(gate)) return;
-    const int nc = prm->ncand;
-    if (static_cast<int>(blockIdx.x) >= nc) return;
-    extern __shared__ float2 left[];  // [n]: (positive, negative) left sums after each position
-    __shared__ RefChunk bufs[2][kRefineGatherWarps];
-    __shared__ float2 totals;
-    __shared__ unsigned long long warpBest[kRefineWarps];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int chunks = (n + 255) / 256;
-    const int sets = (chunks + kRefineGatherWarps - 1) / kRefineGatherWarps;
-    for (int c = blockIdx.x; c < nc; c += gridDim.x) {
-        const int f = cand[c];
-        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride;
-        const uint16_t* grow = gap + static_cast<size_t>(f) * gapStride;
-        float tp = 0.0f, tn = 0.0f;  // the chains (lanes 0 and 1 of warp 7)
-        for (int k = 0; k <= sets; ++k) {
-            if (w < kRefineGatherWarps) {
-                const int i = k * kRefineGatherWarps + w;
-                if (k < sets && i < chunks) {
-                    RefChunk& B = bufs[k & 1][w];
-                    const int k0 = i * 256 + lane * 8;
-                    const uint4 v = k0 < n ? __ldg(reinterpret_cast<const uint4*>(row + ord_slot(k0, L)))
-                                           : make_uint4(0, 0, 0, 0);
-                    const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-                    float e[8];
-#pragma unroll
-                    for (int h = 0; h < 8; ++h) {
-                        uint32_t id = (w4[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
-                        if (kTwoCopy) id = slot_sample(id, slotBase);
-                        e[h] = k0 + h < n ? __ldg(wsgG + id) : 0.0f;
-                    }
-                    uint32_t pm = 0, nm = 0;
-#pragma unroll
-                    for (int h = 0; h < 8; ++h) {
-                        if (k0 + h < n) {
-                            if (signbit(e[h]))
-                                nm |= 1u << h;
-                            else
-                                pm |= 1u << h;
-                        }
-                    }
-                    // exclusive offsets of this lane's addends in the two lists
-                    const uint32_t both = (static_cast<uint32_t>(__popc(pm)) << 16) | static_cast<uint32_t>(__popc(nm));
-                    uint32_t incl = both;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= o) incl += y;
-                    }
-                    uint32_t run = incl - both;
-#pragma unroll
-                    for (int h = 0; h < 8; ++h) {
-                        if ((pm >> h) & 1u) {
-                            B.pos[run >> 16] = fabsf(e[h]);
-                            run += 1u << 16;
-                        } else if ((nm >> h) & 1u) {
-                            B.neg[run & 0xFFFFu] = fabsf(e[h]);
-                            run += 1u;
-                        }
-                        B.cnt[lane * 8 + h] = run;
-                    }
-                    if (lane == 31) {
-                        B.np = static_cast<int>(incl >> 16);
-                        B.nn = static_cast<int>(incl & 0xFFFFu);
-                    }
-                }
-            } else if (k > 0) {
-                // warp 7: the chains of set k - 1, chunk by chunk in order
-                for (int g = 0; g < kRefineGatherWarps; ++g) {
-                    const int i = (k - 1) * kRefineGatherWarps + g;
-                    if (i >= chunks) break;
-                    RefChunk& B = bufs[(k - 1) & 1][g];
-                    const float tpIn = __shfl_sync(0xffffffffu, tp, 0), tnIn = __shfl_sync(0xffffffffu, tn, 1);
-                    if (lane < 2) {
-                        float* list = lane == 0 ? B.pos : B.neg;
-                        const int m = lane == 0 ? B.np : B.nn;
-                        float t = lane == 0 ? tp : tn;
-                        int j0 = 0;
-                        for (; j0 + 8 <= m; j0 += 8) {
-                            float q[8];
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) q[j] = list[j0 + j];
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                t = __fadd_rn(t, q[j]);
-                                q[j] = t;
-                            }
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) list[j0 + j] = q[j];
-                        }
-                        for (; j0 < m; ++j0) {
-                            t = __fadd_rn(t, list[j0]);
-                            list[j0] = t;
-                        }
-                        if (lane == 0)
-                            tp = t;
-                        else
-                            tn = t;
-                    }
-                    __syncwarp();
-                    // every position's left sums: the running sum after its class's
-                    // last addend at or before it, or the chain's value at the chunk's start
-                    const int base = i * 256;
-#pragma unroll
-                    for (int h = 0; h < 8; ++h) {
-                        const int p = lane * 8 + h;
-                        if (base + p < n) {
-                            const uint32_t cc = B.cnt[p];
-                            const uint32_t cp = cc >> 16, cn = cc & 0xFFFFu;
-                            left[base + p] = make_float2(cp ? B.pos[cp - 1] : tpIn, cn ? B.neg[cn - 1] : tnIn);
-                        }
-                    }
-                    __syncwarp();
-                }
-            }
-            __syncthreads();
-        }
-        if (w == kRefineWarps - 1 && lane == 0) totals.x = tp;
-        if (w == kRefineWarps - 1 && lane == 1) totals.y = tn;
-        __syncthreads();
-        const float TP = totals.x, TN = totals.y;
-        // Scoring: the reference's update rule over the splits in order (lower
-        // error replaces; at equal error parity +1 replaces parity -1) picks the
-        // lexicographic minimum of (error, parity +1 before -1, split index);
-        // errors are >= +0, so the float bits order like the values and the
-        // triple packs into one key.  Warp w takes chunks w, w + 8, ...
-        unsigned long long best = ~0ull;
-        for (int i = w; i < chunks; i += kRefineWarps) {
-            const int k0 = i * 256 + lane * 8;
-            if (k0 >= n - 1) continue;
-            const int l = k0 / L, r = k0 - l * L;
-            const uint32_t g = (static_cast<uint32_t>(__ldg(grow + (r >> 4) * 32 + l)) >> (r & 15)) & 0xFFu;  // gap_word
-#pragma unroll
-            for (int h = 0; h < 8; ++h) {
-                if ((g >> h) & 1u) {
-                    const float2 lv = left[k0 + h];
-                    const float eL = __fadd_rn(lv.y, __fsub_rn(TP, lv.x));  // parity -1
-                    const float eR = __fadd_rn(lv.x, __fsub_rn(TN, lv.y));  // parity +1
-                    const unsigned kk = static_cast<unsigned>(k0 + h);
-                    const unsigned long long kL =
-                        (static_cast<unsigned long long>(__float_as_uint(eL)) << 32) | 0x80000000u | kk;
-                    const unsigned long long kR = (static_cast<unsigned long long>(__float_as_uint(eR)) << 32) | kk;
-                    best = min(best, min(kL, kR));
-                }
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-        if (lane == 0) warpBest[w] = best;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int k = 1; k < kRefineWarps; ++k) best = min(best, warpBest[k]);
-            // (error bits, featureIdx) of every candidate, for the runner-up report
-            candKey[c] = best != ~0ull ? (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f) : ~0ull;
-            if (best != ~0ull) {
-                refParity[f] = (best & 0x80000000ull) ? int8_t(-1) : int8_t(1);
-                refSplit[f] = static_cast<int>(best & 0x7FFFFFFFull);
-                atomicMin(&prm->winner, (best & 0xFFFFFFFF00000000ull) | static_cast<unsigned>(f));
-            }
-        }
-        // the buffers and left sums are reused by the CTA's next candidate
-        __syncthreads();
-    }
-}
-
 // The replay with the two class chains decoupled, for n <= kRefineSplitMaxN:
 // one candidate per CTA.  In a candidate's sorted order the classes come in
 // long runs (a good feature separates them), so per-chunk class lists leave
@@ -1583,36 +1388,41 @@ refine_split_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const u
             }
         }
         __syncthreads();
-        // C. the two chains, concurrently
+        // C. the two chains, concurrently: both lanes over the common length
+        // in groups of 4 (the next two groups' loads in flight, the same form
+        // as a lone dependent chain), then the longer list alone, then the
+        // last addends one by one.  Loads past a list's end stay inside the
+        // lists array and are never used.
         if (w == 0 && lane < 2) {
-            const int base = lane == 0 ? 0 : nOff;
+            float* list = lists + (lane == 0 ? 0 : nOff);
             const int mine = lane == 0 ? P : N;
-            const int m4 = (max(P, N) + 3) & ~3;
-            const int last4 = mine > 0 ? ((mine - 1) & ~3) : 0;  // loads stay within the own list
+            const int common = min(P, N) & ~3;
             float t = 0.0f;
-            auto ld = [&](int j) {
-                float4 q = *reinterpret_cast<const float4*>(lists + base + min(j, last4));
-                if (j + 0 >= mine) q.x = 0.0f;
-                if (j + 1 >= mine) q.y = 0.0f;
-                if (j + 2 >= mine) q.z = 0.0f;
-                if (j + 3 >= mine) q.w = 0.0f;
-                return q;
+            auto run = [&](int j, int end) {
+                float4 q0 = *reinterpret_cast<const float4*>(list + j);
+                float4 q1 = *reinterpret_cast<const float4*>(list + j + 4);
+                for (; j < end; j += 4) {
+                    const float4 q2 = *reinterpret_cast<const float4*>(list + j + 8);
+                    float4 r;
+                    t = __fadd_rn(t, q0.x);
+                    r.x = t;
+                    t = __fadd_rn(t, q0.y);
+                    r.y = t;
+                    t = __fadd_rn(t, q0.z);
+                    r.z = t;
+                    t = __fadd_rn(t, q0.w);
+                    r.w = t;
+                    *reinterpret_cast<float4*>(list + j) = r;
+                    q0 = q1;
+                    q1 = q2;
+                }
+                return j;
             };
-            float4 q0 = ld(0), q1 = ld(4);
-            for (int j = 0; j < m4; j += 4) {
-                const float4 q2 = ld(j + 8);
-                float4 r;
-                t = __fadd_rn(t, q0.x);
-                r.x = t;
-                t = __fadd_rn(t, q0.y);
-                r.y = t;
-                t = __fadd_rn(t, q0.z);
-                r.z = t;
-                t = __fadd_rn(t, q0.w);
-                r.w = t;
-                if (j < mine) *reinterpret_cast<float4*>(lists + base + j) = r;
-                q0 = q1;
-                q1 = q2;
+            int j = run(0, common);
+            j = run(j, mine & ~3);
+            for (; j < mine; ++j) {
+                t = __fadd_rn(t, list[j]);
+                list[j] = t;
             }
         }
         __syncthreads();
@@ -2580,15 +2390,6 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
                             t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb, t->laneRun, t->d_prm,
                             t->d_cand, t->d_refParity, t->d_refSplit, t->d_candKey, t->d_gate));
         VJ_LAUNCH_CHECK("refine_split_kernel");
-    } else if (n <= kRefineSharedMaxN) {
-        auto k = sb > 0 ? refine_shared_kernel<true> : refine_shared_kernel<false>;
-        const size_t lbytes = sizeof(float2) * static_cast<size_t>(n);
-        VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lbytes)));
-        VJ_TIMED_LAUNCH("refine_kernel", s,
-                        k<<<refine_blocks(), kRefineThreads, lbytes, s>>>(
-                            t->d_ord, t->ordStride, t->d_gap, t->gapStride, t->d_wsg, n, sb, t->laneRun, t->d_prm,
-                            t->d_cand, t->d_refParity, t->d_refSplit, t->d_candKey, t->d_gate));
-        VJ_LAUNCH_CHECK("refine_shared_kernel");
     } else {
         auto k = smemW ? refine_kernel<true> : refine_kernel<false>;
         VJ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(wbytes)));
