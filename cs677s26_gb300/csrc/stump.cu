@@ -1629,20 +1629,39 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
     const double F = sF;
     const int par = sPar;
     double acc = 0.0;
-    for (int i = t; i < n; i += kRoundPartials) {
-        const float r = train_response(f, sumT, n, i, invNorm[i]);
-        const bool lt = r < theta;
-        strong[i] = __fadd_rn(strong[i], lt ? left : right);
-        const bool act = active == nullptr || active[i] != 0;
-        if (!act) {
-            xbuf[i] = 0.0;
-            continue;
+    // four samples' loads in flight at once; their values are then added to
+    // the partial in sample order, as one sample per step would
+    for (int i0 = t; i0 < n; i0 += 4 * kRoundPartials) {
+        float r[4], sw[4], wt[4];
+        bool act[4];
+        int lab[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * kRoundPartials;
+            if (i < n) {
+                r[u] = train_response(f, sumT, n, i, invNorm[i]);
+                sw[u] = strong[i];
+                act[u] = active == nullptr || active[i] != 0;
+                wt[u] = weight[i];
+                lab[u] = label[i];
+            }
         }
-        const int pred = par > 0 ? (lt ? -1 : 1) : (lt ? 1 : -1);
-        double x = static_cast<double>(weight[i]);
-        if (pred != static_cast<int>(label[i])) x = x * F;
-        xbuf[i] = x;
-        acc += x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * kRoundPartials;
+            if (i >= n) break;
+            const bool lt = r[u] < theta;
+            strong[i] = __fadd_rn(sw[u], lt ? left : right);
+            if (!act[u]) {
+                xbuf[i] = 0.0;
+                continue;
+            }
+            const int pred = par > 0 ? (lt ? -1 : 1) : (lt ? 1 : -1);
+            double x = static_cast<double>(wt[u]);
+            if (pred != lab[u]) x = x * F;
+            xbuf[i] = x;
+            acc += x;
+        }
     }
     partials[t] = acc;
 }
@@ -1711,14 +1730,40 @@ stage_calib_kernel(const float* __restrict__ strong, const uint8_t* __restrict__
             if ((k & himask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
         }
         __syncthreads();
-        if (tid == 0) {
-            uint32_t kk = sK, d = 0;
-            while (d < 255 && hist[d] <= kk) {
-                kk -= hist[d];
-                ++d;
+        // The digit: the first d < 255 whose inclusive count C(d) exceeds
+        // the rank k (else 255), and the rank within it k - C(d - 1).  Warp
+        // 0 scans the 256 counts, 8 consecutive digits per lane.
+        if (tid < 32) {
+            const uint32_t kk = sK;
+            uint32_t h[8], sum = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                h[j] = hist[tid * 8 + j];
+                sum += h[j];
             }
-            sK = kk;
-            sPrefix = prefix | (d << shift);
+            uint32_t incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (tid >= o) incl += y;
+            }
+            const unsigned over = __ballot_sync(0xffffffffu, incl > kk);
+            const int lane = over ? __ffs(over) - 1 : 31;
+            if (tid == lane) {
+                uint32_t run = incl - sum, d = static_cast<uint32_t>(tid * 8);
+                int j = 0;
+                while (j < 7 && d < 255u && run + h[j] <= kk) {
+                    run += h[j];
+                    ++d;
+                    ++j;
+                }
+                if (d < 255u && run + h[j] <= kk) {  // lane 31 past its last digit: capped at 255
+                    run += h[j];
+                    ++d;
+                }
+                sK = kk - run;
+                sPrefix = prefix | (d << shift);
+            }
         }
         __syncthreads();
     }
