@@ -968,36 +968,54 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
         }
     };
     // Used features are skipped when reached, so no load waits on the mask.
-    auto load = [&](int f, int t, uint4& a, uint4& b, uint32_t& g) {
-        a = b = make_uint4(z, z, z, z);
-        g = 0;
-        if (f < 0) return;
-        const int k0 = lane * L + 16 * t;
-        const uint16_t* row = ord + static_cast<size_t>(f) * ordStride + 512 * t + lane * 8;  // ord_slot(k0, L)
-        if (k0 < n) a = __ldg(reinterpret_cast<const uint4*>(row));
-        if (k0 + 8 < n) b = __ldg(reinterpret_cast<const uint4*>(row + 256));
-        if (k0 < n - 1) g = __ldg(gap + static_cast<size_t>(f) * gapStride + 32 * t + lane);  // gap_word(k0, L)
+    // A cursor is a (feature, step) item with the addresses of its order and
+    // bitmask words; stepping within a feature only moves the addresses.
+    struct Cursor {
+        int f, t, k0;
+        const uint16_t* row;  // ord_slot(k0, L) of this lane
+        const uint16_t* gw;   // gap_word(k0, L) of this lane
     };
-    auto advance = [&](int& f, int& t) {
-        if (f < 0) return;
-        if (++t == spf) {
-            t = 0;
-            f = next_feature();
+    auto start = [&](Cursor& c, int f) {
+        c.f = f;
+        c.t = 0;
+        c.k0 = lane * L;
+        if (f >= 0) {
+            c.row = ord + static_cast<size_t>(f) * ordStride + lane * 8;
+            c.gw = gap + static_cast<size_t>(f) * gapStride + lane;
         }
     };
-    int f = next_feature(), t = 0;  // item being processed
-    int fn = f, tn = t;             // item being loaded
-    advance(fn, tn);
+    auto load = [&](const Cursor& c, uint4& a, uint4& b, uint32_t& g) {
+        a = b = make_uint4(z, z, z, z);
+        g = 0;
+        if (c.f < 0) return;
+        if (c.k0 < n) a = __ldg(reinterpret_cast<const uint4*>(c.row));
+        if (c.k0 + 8 < n) b = __ldg(reinterpret_cast<const uint4*>(c.row + 256));
+        if (c.k0 < n - 1) g = __ldg(c.gw);
+    };
+    auto advance = [&](Cursor& c) {
+        if (c.f < 0) return;
+        if (++c.t == spf) {
+            start(c, next_feature());
+        } else {
+            c.k0 += 16;
+            c.row += 512;
+            c.gw += 32;
+        }
+    };
+    Cursor cur, nxt;  // the item being processed, the item being loaded
+    start(cur, next_feature());
+    nxt = cur;
+    advance(nxt);
     uint4 ca, cb;
     uint32_t cg;
-    load(f, t, ca, cb, cg);
+    load(cur, ca, cb, cg);
     float carry = 0.0f, comp = 0.0f, pmin = INFINITY, pmax = -INFINITY;
-    while (f >= 0) {
+    while (cur.f >= 0) {
         uint4 na, nb;
         uint32_t ng;
-        load(fn, tn, na, nb, ng);
-        int fa = fn, ta = tn;  // the item after the one being loaded
-        advance(fa, ta);
+        load(nxt, na, nb, ng);
+        Cursor aft = nxt;  // the item after the one being loaded
+        advance(aft);
         const uint32_t w8[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
         float s = 0.0f, lmin = INFINITY, lmax = -INFINITY;
 #pragma unroll
@@ -1008,17 +1026,17 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
                 lmax = fmaxf(lmax, s);
             }
         }
-        if (lmax > -INFINITY) {
-            pmin = fminf(pmin, __fadd_rn(carry, lmin));
-            pmax = fmaxf(pmax, __fadd_rn(carry, lmax));
-        }
+        // a step without a valid split leaves lmin = +inf and lmax = -inf,
+        // which the carry keeps infinite and the merge ignores
+        pmin = fminf(pmin, __fadd_rn(carry, lmin));
+        pmax = fmaxf(pmax, __fadd_rn(carry, lmax));
         {
             const float y = __fsub_rn(s, comp);
             const float u = __fadd_rn(carry, y);
             comp = __fsub_rn(__fsub_rn(u, carry), y);
             carry = u;
         }
-        if (t == spf - 1) {
+        if (cur.t == spf - 1) {
             // exclusive prefix of the lanes' run sums
             float incl = carry;
 #pragma unroll
@@ -1041,10 +1059,10 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
             float best = INFINITY;
             if (hi > -INFINITY) best = fmaxf(fminf(__fsub_rn(TP, hi), __fadd_rn(TN, lo)), 0.0f);
             if (lane == 0) {
-                fastErr[f] = best;
+                fastErr[cur.f] = best;
                 // exact best error >= fast error - bfast; +inf for no valid split,
                 // which no later round of the stage can change
-                lb[f] = fmaxf(__fsub_rd(best, bfast), 0.0f);
+                lb[cur.f] = fmaxf(__fsub_rd(best, bfast), 0.0f);
                 if (best < runMin) atomicMin(&prm->fastMinBits, __float_as_uint(best));
                 ++swept;
             }
@@ -1053,10 +1071,8 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
             pmin = INFINITY;
             pmax = -INFINITY;
         }
-        f = fn;
-        t = tn;
-        fn = fa;
-        tn = ta;
+        cur = nxt;
+        nxt = aft;
         ca = na;
         cb = nb;
         cg = ng;
