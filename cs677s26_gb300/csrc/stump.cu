@@ -1002,20 +1002,22 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
             c.gw += 32;
         }
     };
-    Cursor cur, nxt;  // the item being processed, the item being loaded
-    start(cur, next_feature());
-    nxt = cur;
-    advance(nxt);
-    uint4 ca, cb;
-    uint32_t cg;
-    load(cur, ca, cb, cg);
+    // The loop is unrolled twice so that the two sets of item registers
+    // alternate between "being processed" and "being loaded" without copies.
+    Cursor ld;  // the item being loaded
+    start(ld, next_feature());
+    int pf = ld.f;                   // feature of the item being processed, -1 at the end
+    bool plast = ld.t == spf - 1;    // the item is its feature's last step
+    uint4 a0, b0, a1, b1;
+    uint32_t g0, g1;
+    load(ld, a0, b0, g0);
+    advance(ld);
     float carry = 0.0f, comp = 0.0f, pmin = INFINITY, pmax = -INFINITY;
-    while (cur.f >= 0) {
-        uint4 na, nb;
-        uint32_t ng;
-        load(nxt, na, nb, ng);
-        Cursor aft = nxt;  // the item after the one being loaded
-        advance(aft);
+    auto step = [&](const uint4& ca, const uint4& cb, const uint32_t cg, uint4& na, uint4& nb, uint32_t& ng) {
+        const int qf = ld.f;
+        const bool qlast = ld.t == spf - 1;
+        load(ld, na, nb, ng);
+        advance(ld);
         const uint32_t w8[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
         float s = 0.0f, lmin = INFINITY, lmax = -INFINITY;
 #pragma unroll
@@ -1036,7 +1038,7 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
             comp = __fsub_rn(__fsub_rn(u, carry), y);
             carry = u;
         }
-        if (cur.t == spf - 1) {
+        if (plast) {
             // exclusive prefix of the lanes' run sums
             float incl = carry;
 #pragma unroll
@@ -1059,10 +1061,10 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
             float best = INFINITY;
             if (hi > -INFINITY) best = fmaxf(fminf(__fsub_rn(TP, hi), __fadd_rn(TN, lo)), 0.0f);
             if (lane == 0) {
-                fastErr[cur.f] = best;
+                fastErr[pf] = best;
                 // exact best error >= fast error - bfast; +inf for no valid split,
                 // which no later round of the stage can change
-                lb[cur.f] = fmaxf(__fsub_rd(best, bfast), 0.0f);
+                lb[pf] = fmaxf(__fsub_rd(best, bfast), 0.0f);
                 if (best < runMin) atomicMin(&prm->fastMinBits, __float_as_uint(best));
                 ++swept;
             }
@@ -1071,11 +1073,13 @@ sweep_kernel(const uint16_t* __restrict__ ord, int64_t ordStride, const uint16_t
             pmin = INFINITY;
             pmax = -INFINITY;
         }
-        cur = nxt;
-        nxt = aft;
-        ca = na;
-        cb = nb;
-        cg = ng;
+        pf = qf;
+        plast = qlast;
+    };
+    while (pf >= 0) {
+        step(a0, b0, g0, a1, b1, g1);
+        if (pf < 0) break;
+        step(a1, b1, g1, a0, b0, g0);
     }
     if (lane == 0 && swept) {
         atomicAdd(&prm->swept, swept);
