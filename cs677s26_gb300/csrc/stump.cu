@@ -246,7 +246,8 @@ constexpr size_t sort_smem_bytes() {
 // (slots, padding).
 __device__ __forceinline__ void sort_epilogue(const uint32_t* keys, uint16_t* idx, uint32_t* gnat, int n, int fl,
                                               uint16_t* __restrict__ ordOut, int64_t ordStride, bool ordPadded,
-                                              uint16_t* __restrict__ gapOut, int64_t gapStride, int slotBase, int L) {
+                                              uint16_t* __restrict__ gapOut, int64_t gapStride, int slotBase, int L,
+                                              uint16_t* stage = nullptr, int stageCap = 0) {
     const int tid = threadIdx.x;
     // Valid split positions: v[k] + 1e-7f < v[k+1] (boosting_core.cu:400).
     // One thread per unit of 16 consecutive positions: the unit's order
@@ -295,21 +296,18 @@ __device__ __forceinline__ void sort_epilogue(const uint32_t* keys, uint16_t* id
         for (int g = tid; g < L; g += kSortThreads) {
             const int kb = 16 * (g >> 4) + (g & 15);
             const int members = kb < n ? min(32, (n - kb + L - 1) / L) : 0;  // kb + m*L < n
-            uint32_t cur[8], nxt[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) cur[i] = i < members ? idx[kb + i * L] : 0u;
             uint32_t o1 = 0, o2 = 0;
+            auto read8 = [&](uint32_t (&x)[8], int m0) {
 #pragma unroll
-            for (int m0 = 0; m0 < 32; m0 += 8) {
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    nxt[i] = (m0 + 8 < 32 && m0 + 8 + i < members) ? idx[kb + (m0 + 8 + i) * L] : 0u;
+                for (int i = 0; i < 8; ++i) x[i] = m0 + i < members ? idx[kb + (m0 + i) * L] : 0u;
+            };
+            auto decide8 = [&](const uint32_t (&x)[8], int m0) {
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const int m = m0 + i;
                     if (m < members) {
-                        const uint32_t off1 = copy1_offset(cur[i]);
-                        const int b0 = cur[i] & 31, b1 = off1 & 31;
+                        const uint32_t off1 = copy1_offset(x[i]);
+                        const int b0 = x[i] & 31, b1 = off1 & 31;
                         // copy 1 when its bank is strictly less loaded
                         const uint32_t l0 = ((o1 >> b0) & 1u) + ((o2 >> b0) & 1u);
                         const uint32_t l1 = ((o1 >> b1) & 1u) + ((o2 >> b1) & 1u);
@@ -320,20 +318,49 @@ __device__ __forceinline__ void sort_epilogue(const uint32_t* keys, uint16_t* id
                         if (one) idx[kb + m * L] = static_cast<uint16_t>(slotBase + off1);
                     }
                 }
-#pragma unroll
-                for (int i = 0; i < 8; ++i) cur[i] = nxt[i];
-            }
+            };
+            // two register sets of 8 members in turn, each refilled while the
+            // other is decided
+            uint32_t xa[8], xb[8];
+            read8(xa, 0);
+            read8(xb, 8);
+            decide8(xa, 0);
+            read8(xa, 16);
+            decide8(xb, 8);
+            read8(xb, 24);
+            decide8(xa, 16);
+            decide8(xb, 24);
         }
         __syncthreads();
     }
-    // Sorted sample order (padded rows: lane runs, see ord_slot).
+    // Sorted sample order (padded rows: lane runs, see ord_slot).  With room
+    // in `stage`, the row is first laid out there (each 256-entry block of
+    // the row padded by 8 entries, so neither the scattered 16-byte writes
+    // nor the reads conflict) and then copied out 512 contiguous bytes per
+    // warp instruction; the positions past n carry the zero slot.
     uint16_t* orow = ordOut + static_cast<size_t>(fl) * ordStride;
     if (ordPadded) {
         const int n8 = (n + 7) & ~7;
         if (tid < n8 - n) idx[n + tid] = static_cast<uint16_t>(zero_slot(n, slotBase));
         __syncthreads();
-        for (int k = tid * 8; k < n8; k += kSortThreads * 8)
-            *reinterpret_cast<uint4*>(orow + ord_slot(k, L)) = *reinterpret_cast<const uint4*>(idx + k);
+        const int blocks = L / 8;  // 256-entry blocks of the 32 L entries
+        if (stage != nullptr && blocks * 264 <= stageCap) {
+            const uint32_t zz = static_cast<uint32_t>(zero_slot(n, slotBase)) * 0x10001u;
+            for (int k = tid * 8; k < 32 * L; k += kSortThreads * 8) {
+                const int o = ord_slot(k, L);
+                *reinterpret_cast<uint4*>(stage + o + 8 * (o >> 8)) =
+                    k < n8 ? *reinterpret_cast<const uint4*>(idx + k) : make_uint4(zz, zz, zz, zz);
+            }
+            __syncthreads();
+            for (int j = tid; j < blocks * 32; j += kSortThreads) {
+                const int b = j >> 5, l = j & 31;
+                *reinterpret_cast<uint4*>(orow + b * 256 + l * 8) =
+                    *reinterpret_cast<const uint4*>(stage + b * 264 + l * 8);
+            }
+        } else {
+            for (int k = tid * 8; k < n8; k += kSortThreads * 8)
+                *reinterpret_cast<uint4*>(orow + ord_slot(k, L)) = *reinterpret_cast<const uint4*>(idx + k);
+        }
     } else {
         for (int k = tid; k < n; k += kSortThreads) orow[k] = idx[k];
     }
@@ -446,7 +473,8 @@ eval_sort_kernel(const vj_haar_feature* __restrict__ feats, int featBegin, int f
             __syncthreads();
         }
 
-        sort_epilogue(keys, idx, cnt, n, fl, ordOut, ordStride, ordPadded, gapOut, gapStride, slotBase, L);
+        sort_epilogue(keys, idx, cnt, n, fl, ordOut, ordStride, ordPadded, gapOut, gapStride, slotBase, L,
+                      reinterpret_cast<uint16_t*>(cnt), 256 * kCntStride * 2);
         __syncthreads();
     }
 }
@@ -619,7 +647,8 @@ eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegi
             }
             __syncthreads();
         }
-        sort_epilogue(keys, idxB, cnt, n, fl, ordOut, ordStride, ordPadded, gapOut, gapStride, slotBase, L);
+        sort_epilogue(keys, idxB, cnt, n, fl, ordOut, ordStride, ordPadded, gapOut, gapStride, slotBase, L,
+                      reinterpret_cast<uint16_t*>(cnt), kCntRows * kCntRow * 2);
         __syncthreads();
     }
 }
