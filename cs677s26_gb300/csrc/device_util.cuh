@@ -68,6 +68,49 @@ __device__ __forceinline__ float train_response(const vj_haar_feature& f, const 
     return __fmul_rn(resp, invNorm);
 }
 
+// Corners that a feature's rectangles share, for the response evaluation:
+// the same train_response arithmetic with each shared corner loaded once.
+//   1: two rectangles, r1.p1 = r0.p1 and r1.p3 = r0.p3;
+//   2: two rectangles, r1.p2 = r0.p2 and r1.p3 = r0.p3;
+//   3: three rectangles, r1.p0 = r0.p0, r2.p0 = r1.p3 and r2.p3 = r0.p3;
+//   0: anything else (every corner loaded).
+// The three shapes cover every non-tilted Basic, Core and All feature that
+// shares a corner.
+__host__ __device__ __forceinline__ int corner_sharing(const vj_haar_feature& f) {
+    if (f.rectCount == 2) {
+        if (f.r1.p1 == f.r0.p1 && f.r1.p3 == f.r0.p3) return 1;
+        if (f.r1.p2 == f.r0.p2 && f.r1.p3 == f.r0.p3) return 2;
+    } else if (f.rectCount == 3) {
+        if (f.r1.p0 == f.r0.p0 && f.r2.p0 == f.r1.p3 && f.r2.p3 == f.r0.p3) return 3;
+    }
+    return 0;
+}
+
+// train_response for a feature of corner_sharing(f) == S.
+template <int S>
+__device__ __forceinline__ float train_response_shared(const vj_haar_feature& f, const uint32_t* __restrict__ sumT,
+                                                       int n, int s, float invNorm) {
+    if (S == 0) return train_response(f, sumT, n, s, invNorm);
+    const size_t N = static_cast<size_t>(n);
+    auto ld = [&](int p) { return corner_f(__ldg(sumT + static_cast<size_t>(p) * N + s)); };
+    auto rect = [](float a, float b, float c, float d) { return __fadd_rn(__fsub_rn(__fsub_rn(a, b), c), d); };
+    const float a0 = ld(f.r0.p0), a1 = ld(f.r0.p1), a2 = ld(f.r0.p2), a3 = ld(f.r0.p3);
+    float resp;
+    if (S == 1) {
+        const float b0 = ld(f.r1.p0), b2 = ld(f.r1.p2);
+        resp = __fadd_rn(__fmul_rn(f.r0.w, rect(a0, a1, a2, a3)), __fmul_rn(f.r1.w, rect(b0, a1, b2, a3)));
+    } else if (S == 2) {
+        const float b0 = ld(f.r1.p0), b1 = ld(f.r1.p1);
+        resp = __fadd_rn(__fmul_rn(f.r0.w, rect(a0, a1, a2, a3)), __fmul_rn(f.r1.w, rect(b0, b1, a2, a3)));
+    } else {
+        const float b1 = ld(f.r1.p1), b2 = ld(f.r1.p2), b3 = ld(f.r1.p3);
+        const float c1 = ld(f.r2.p1), c2 = ld(f.r2.p2);
+        resp = __fadd_rn(__fmul_rn(f.r0.w, rect(a0, a1, a2, a3)), __fmul_rn(f.r1.w, rect(a0, b1, b2, b3)));
+        resp = __fadd_rn(resp, __fmul_rn(f.r2.w, rect(b3, c1, c2, a3)));
+    }
+    return __fmul_rn(resp, invNorm);
+}
+
 inline int div_up(int64_t a, int64_t b) { return static_cast<int>((a + b - 1) / b); }
 
 }  // namespace vjgb

@@ -39,6 +39,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "device_util.cuh"
@@ -590,18 +591,29 @@ eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegi
             if (tid == 0) sfeat = feats[featBegin + fl];
             __syncthreads();
             const vj_haar_feature& f = sfeat;
-            for (int s0 = tid; s0 < NP; s0 += 4 * kSortThreads) {
-                float r[4];
+            // four samples per thread in flight; each corner a feature's
+            // rectangles share is loaded once (corner_sharing)
+            auto eval = [&](auto shape) {
+                constexpr int S = decltype(shape)::value;
+                for (int s0 = tid; s0 < NP; s0 += 4 * kSortThreads) {
+                    float r[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int s = s0 + u * kSortThreads;
-                    r[u] = s < n ? train_response(f, sumT, n, s, __ldg(invNorm + s)) : 0.0f;
-                }
+                    for (int u = 0; u < 4; ++u) {
+                        const int s = s0 + u * kSortThreads;
+                        r[u] = s < n ? train_response_shared<S>(f, sumT, n, s, __ldg(invNorm + s)) : 0.0f;
+                    }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int s = s0 + u * kSortThreads;
-                    if (s < NP) keys[s] = s < n ? radix_key(__float_as_uint(r[u])) : ~0u;
+                    for (int u = 0; u < 4; ++u) {
+                        const int s = s0 + u * kSortThreads;
+                        if (s < NP) keys[s] = s < n ? radix_key(__float_as_uint(r[u])) : ~0u;
+                    }
                 }
+            };
+            switch (corner_sharing(f)) {
+                case 1: eval(std::integral_constant<int, 1>()); break;
+                case 2: eval(std::integral_constant<int, 2>()); break;
+                case 3: eval(std::integral_constant<int, 3>()); break;
+                default: eval(std::integral_constant<int, 0>()); break;
             }
         }
         __syncthreads();
