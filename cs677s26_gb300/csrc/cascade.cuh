@@ -10,6 +10,8 @@
 // results equal the reference CPU path bit for bit.
 #pragma once
 
+#include <type_traits>
+
 #include "group_dev.cuh"
 #include "integral_dev.cuh"
 
@@ -403,6 +405,45 @@ __device__ __forceinline__ float decoded_value(const LevelStump& d, const uint32
     return __fmul_rn(raw, inv) < d.theta ? d.left : d.right;
 }
 
+// Corners that a decoded stump's rectangles share (equal offsets), the
+// shapes of corner_sharing: 1 (2 rects, r1.p1 = r0.p1, r1.p3 = r0.p3),
+// 2 (2 rects, r1.p2 = r0.p2, r1.p3 = r0.p3), 3 (3 rects, r1.p0 = r0.p0,
+// r2.p0 = r1.p3, r2.p3 = r0.p3), 0 otherwise.
+__device__ __forceinline__ int decoded_sharing(const LevelStump& d) {
+    if (d.nr == 2) {
+        if (d.off[5] == d.off[1] && d.off[7] == d.off[3]) return 1;
+        if (d.off[6] == d.off[2] && d.off[7] == d.off[3]) return 2;
+    } else if (d.nr == 3) {
+        if (d.off[4] == d.off[0] && d.off[8] == d.off[7] && d.off[11] == d.off[3]) return 3;
+    }
+    return 0;
+}
+
+// decoded_value for a stump of decoded_sharing shape S: each shared corner
+// gathered once, the same operations in the same order.
+template <int S>
+__device__ __forceinline__ float decoded_value_shared(const LevelStump& d, const uint32_t* sum, int b, float inv) {
+    if (S == 0) return decoded_value(d, sum, b, inv);
+    auto ld = [&](int q) { return corner_f(sum[b + d.off[q]]); };
+    auto rect = [](float c0, float c1, float c2, float c3, float w) {
+        return __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(c0, c1), c2), c3), w);
+    };
+    const float a0 = ld(0), a1 = ld(1), a2 = ld(2), a3 = ld(3);
+    float raw;
+    if (S == 1) {
+        const float b0 = ld(4), b2 = ld(6);
+        raw = __fadd_rn(rect(a0, a1, a2, a3, d.w[0]), rect(b0, a1, b2, a3, d.w[1]));
+    } else if (S == 2) {
+        const float b0 = ld(4), b1 = ld(5);
+        raw = __fadd_rn(rect(a0, a1, a2, a3, d.w[0]), rect(b0, b1, a2, a3, d.w[1]));
+    } else {
+        const float b1 = ld(5), b2 = ld(6), b3 = ld(7), e1 = ld(9), e2 = ld(10);
+        raw = __fadd_rn(rect(a0, a1, a2, a3, d.w[0]), rect(a0, b1, b2, b3, d.w[1]));
+        raw = __fadd_rn(raw, rect(b3, e1, e2, a3, d.w[2]));
+    }
+    return __fmul_rn(raw, inv) < d.theta ? d.left : d.right;
+}
+
 // Leaf value of stump k from the window's integral patch in shared memory
 // (corners already converted to float).
 __device__ __forceinline__ float patch_stump_value(const PStumpPlanes& ps, int k, const float* patch, float inv) {
@@ -574,9 +615,19 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
                     for (int k = 0; k < st.ntrees; ++k) {
                         LevelStump d;
                         decode_stump(P.stumps + st.first + k, pitch, d);
+                        // the stump is the same in every lane: one branch per stump
+                        auto eval4 = [&](auto shape) {
+                            constexpr int S = decltype(shape)::value;
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            if (q < ng) acc[q] = __fadd_rn(acc[q], decoded_value(d, sum, b[q], inv[q]));
+                            for (int q = 0; q < 4; ++q)
+                                if (q < ng) acc[q] = __fadd_rn(acc[q], decoded_value_shared<S>(d, sum, b[q], inv[q]));
+                        };
+                        switch (decoded_sharing(d)) {
+                            case 1: eval4(std::integral_constant<int, 1>()); break;
+                            case 2: eval4(std::integral_constant<int, 2>()); break;
+                            case 3: eval4(std::integral_constant<int, 3>()); break;
+                            default: eval4(std::integral_constant<int, 0>()); break;
+                        }
                     }
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {

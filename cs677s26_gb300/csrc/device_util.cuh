@@ -111,6 +111,43 @@ __device__ __forceinline__ float train_response_shared(const vj_haar_feature& f,
     return __fmul_rn(resp, invNorm);
 }
 
+// train_response of the two consecutive samples s, s+1 (s even, sumT and
+// invNorm 8-byte aligned, n even), each corner of corner_sharing shape S read
+// once as one 8-byte load for both samples; every sample's arithmetic is
+// train_response's.
+template <int S>
+__device__ __forceinline__ float2 train_response2(const vj_haar_feature& f, const uint32_t* __restrict__ sumT, int n,
+                                                  int s, float2 inv) {
+    static_assert(S >= 1 && S <= 3, "a sharing shape; the generic form reads every corner one sample at a time");
+    const size_t N = static_cast<size_t>(n);
+    auto ld = [&](int p) { return __ldg(reinterpret_cast<const uint2*>(sumT + static_cast<size_t>(p) * N + s)); };
+    // the corners in train_response's order (r0.p0..p3, r1.p0..p3, r2.p0..p3)
+    uint2 c[12];
+    c[0] = ld(f.r0.p0);
+    c[1] = ld(f.r0.p1);
+    c[2] = ld(f.r0.p2);
+    c[3] = ld(f.r0.p3);
+    c[4] = S == 3 ? c[0] : ld(f.r1.p0);
+    c[5] = S == 1 ? c[1] : ld(f.r1.p1);
+    c[6] = S == 2 ? c[2] : ld(f.r1.p2);
+    c[7] = (S == 1 || S == 2) ? c[3] : ld(f.r1.p3);
+    constexpr bool three = S == 3;
+    if (three) {
+        c[8] = c[7];
+        c[9] = ld(f.r2.p1);
+        c[10] = ld(f.r2.p2);
+        c[11] = c[3];
+    }
+    auto one = [&](int j, float iv) {
+        auto cf = [&](int q) { return corner_f(j == 0 ? c[q].x : c[q].y); };
+        auto rect = [&](int q) { return __fadd_rn(__fsub_rn(__fsub_rn(cf(q), cf(q + 1)), cf(q + 2)), cf(q + 3)); };
+        float resp = __fadd_rn(__fmul_rn(f.r0.w, rect(0)), __fmul_rn(f.r1.w, rect(4)));
+        if (three) resp = __fadd_rn(resp, __fmul_rn(f.r2.w, rect(8)));
+        return __fmul_rn(resp, iv);
+    };
+    return make_float2(one(0, inv.x), one(1, inv.y));
+}
+
 inline int div_up(int64_t a, int64_t b) { return static_cast<int>((a + b - 1) / b); }
 
 }  // namespace vjgb

@@ -592,9 +592,36 @@ eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegi
             __syncthreads();
             const vj_haar_feature& f = sfeat;
             // four samples per thread in flight; each corner a feature's
-            // rectangles share is loaded once (corner_sharing)
+            // rectangles share is loaded once (corner_sharing); with n even
+            // and aligned tables, a thread's samples come in consecutive
+            // pairs and each corner is one 8-byte load for a pair
+            const bool vec2 = (n & 1) == 0 && (reinterpret_cast<uintptr_t>(sumT) & 7) == 0 &&
+                              (reinterpret_cast<uintptr_t>(invNorm) & 7) == 0;
             auto eval = [&](auto shape) {
                 constexpr int S = decltype(shape)::value;
+                if constexpr (S != 0) {
+                if (vec2) {
+                    for (int s0 = 2 * tid; s0 < NP; s0 += 4 * kSortThreads) {
+                        float2 r[2];
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const int s = s0 + u * 2 * kSortThreads;
+                            r[u] = s < n ? train_response2<S>(f, sumT, n, s,
+                                                              __ldg(reinterpret_cast<const float2*>(invNorm + s)))
+                                         : make_float2(0.0f, 0.0f);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const int s = s0 + u * 2 * kSortThreads;
+                            if (s < NP)
+                                *reinterpret_cast<uint2*>(keys + s) =
+                                    s < n ? make_uint2(radix_key(__float_as_uint(r[u].x)), radix_key(__float_as_uint(r[u].y)))
+                                          : make_uint2(~0u, ~0u);
+                        }
+                    }
+                    return;
+                }
+                }
                 for (int s0 = tid; s0 < NP; s0 += 4 * kSortThreads) {
                     float r[4];
 #pragma unroll
