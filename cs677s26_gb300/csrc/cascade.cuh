@@ -451,18 +451,27 @@ __device__ __forceinline__ float patch_stump_value(const PStumpPlanes& ps, int k
     const uint4 b = __ldg(ps.b + k);
     const uint4 c = __ldg(ps.c + k);
     const float w1 = __uint_as_float(b.x), w2 = __uint_as_float(b.y);
-    const float v0 = __fmul_rn(
-        __fadd_rn(__fsub_rn(__fsub_rn(patch[b.z & 0xFFFFu], patch[b.z >> 16]), patch[b.w & 0xFFFFu]), patch[b.w >> 16]),
-        a.w);
-    const float v1 = __fmul_rn(
-        __fadd_rn(__fsub_rn(__fsub_rn(patch[c.x & 0xFFFFu], patch[c.x >> 16]), patch[c.y & 0xFFFFu]), patch[c.y >> 16]),
-        w1);
+    // A corner at the same offset as an earlier one (the shapes of
+    // corner_sharing: r1.p0 = r0.p0, r1.p1 = r0.p1, r1.p2 = r0.p2,
+    // r1.p3 = r0.p3, r2.p0 = r1.p3, r2.p3 = r0.p3) takes that corner's value
+    // instead of a second shared-memory read; the values are the same.
+    const uint32_t o0 = b.z & 0xFFFFu, o1 = b.z >> 16, o2 = b.w & 0xFFFFu, o3 = b.w >> 16;
+    const uint32_t o4 = c.x & 0xFFFFu, o5 = c.x >> 16, o6 = c.y & 0xFFFFu, o7 = c.y >> 16;
+    const float p0 = patch[o0], p1 = patch[o1], p2 = patch[o2], p3 = patch[o3];
+    float p4, p5, p6, p7;
+    if (o4 == o0) p4 = p0; else p4 = patch[o4];
+    if (o5 == o1) p5 = p1; else p5 = patch[o5];
+    if (o6 == o2) p6 = p2; else p6 = patch[o6];
+    if (o7 == o3) p7 = p3; else p7 = patch[o7];
+    const float v0 = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(p0, p1), p2), p3), a.w);
+    const float v1 = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(p4, p5), p6), p7), w1);
     float raw = __fadd_rn(v0, v1);
     if (w2 != 0.0f) {
-        const float v2 = __fmul_rn(
-            __fadd_rn(__fsub_rn(__fsub_rn(patch[c.z & 0xFFFFu], patch[c.z >> 16]), patch[c.w & 0xFFFFu]),
-                      patch[c.w >> 16]),
-            w2);
+        const uint32_t o8 = c.z & 0xFFFFu, o9 = c.z >> 16, o10 = c.w & 0xFFFFu, o11 = c.w >> 16;
+        float p8, p11;
+        if (o8 == o7) p8 = p7; else p8 = patch[o8];
+        if (o11 == o3) p11 = p3; else p11 = patch[o11];
+        const float v2 = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(p8, patch[o9]), patch[o10]), p11), w2);
         raw = __fadd_rn(raw, v2);
     }
     return __fmul_rn(raw, inv) < a.x ? a.y : a.z;
