@@ -742,6 +742,7 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
     int qi = -1;  // queue index of the slot's window, -1 = empty
     QEntry e{};
     int si = 0, k0 = 0;
+    DStage st{0, 0, 0.0f, 0.0f};  // P.stages[si], read when si changes
     float acc = 0.0f, lacc = 0.0f, score = 0.0f;
     bool exact = false;  // the slot replays its stage with the sequential sum
     bool more = true;
@@ -779,6 +780,7 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
                 qi = static_cast<int>(t);
                 e = ne;
                 si = P.deepFrom;
+                st = P.stages[si];
                 k0 = 0;
                 acc = 0.0f;
                 lacc = 0.0f;
@@ -789,8 +791,6 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
         if (!__any_sync(0xffffffffu, qi >= 0)) break;
         __syncwarp();
         const bool active = qi >= 0;
-        DStage st{0, 0, 0.0f, 0.0f};
-        if (active) st = P.stages[si];
         float c[kDeepEvals];
 #pragma unroll
         for (int ev = 0; ev < kDeepEvals; ++ev) {
@@ -853,6 +853,7 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
                     ++si;
                     k0 = 0;
                     acc = 0.0f;
+                    if (si < P.nStages) st = P.stages[si];
                     if (si >= P.nStages) {
                         if (j == 0) {
                             const CasLevel& L = P.levels[e.level];
