@@ -15,6 +15,7 @@
 // path's order (level, y, x), truncates to maxDetections and groups them
 // (groupRectangles, face_vision_engine.cu:1401-1539).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -175,6 +176,7 @@ struct vj_detector {
     // Work buffers, grown on demand.
     DBuf imgs, pix, iiSum, iiSq, totS, totQ, qA, qB, dets, dplan, dctrl, ghist;
     HBuf hplan, hctrl, hdets;
+    HBuf himgs;  // pinned staging of a large batch's host images, laid out as `imgs`
     int imageCap = 0;  // images the control block has room for
     // Optional arena (vj_detector_reserve): every work buffer of a batch is a
     // range of it, so the detector never holds more than its reservation.
@@ -396,6 +398,42 @@ struct BatchImage {
     int64_t stride;
 };
 
+constexpr int64_t kStageImageBytes = int64_t(16) << 20;
+
+// Copies the images' rows into `dst` at pitch align_up(w, 16) from offset
+// off[i], on up to 16 host threads taking blocks of about 2 MB of rows.
+void stage_images(const std::vector<BatchImage>& ims, const std::vector<int64_t>& off, uint8_t* dst) {
+    struct Piece {
+        int img, r0, r1;
+    };
+    std::vector<Piece> pieces;
+    for (int i = 0; i < static_cast<int>(ims.size()); ++i) {
+        const int rowsPer = std::max(1, static_cast<int>((int64_t(2) << 20) / std::max(1, ims[i].w)));
+        for (int r = 0; r < ims[i].h; r += rowsPer) pieces.push_back({i, r, std::min(ims[i].h, r + rowsPer)});
+    }
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t k; (k = next.fetch_add(1)) < pieces.size();) {
+            const Piece& pc = pieces[k];
+            const BatchImage& im = ims[pc.img];
+            const int64_t pitch = align_up(static_cast<int64_t>(im.w), 16);
+            uint8_t* d = dst + off[pc.img] + pitch * pc.r0;
+            const uint8_t* src = im.ptr + im.stride * pc.r0;
+            if (im.stride == pitch) {
+                std::memcpy(d, src, static_cast<size_t>(pitch) * (pc.r1 - pc.r0 - 1) + im.w);
+            } else {
+                for (int r = pc.r0; r < pc.r1; ++r, d += pitch, src += im.stride) std::memcpy(d, src, im.w);
+            }
+        }
+    };
+    const int T = static_cast<int>(std::min<size_t>(
+        pieces.size(), std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; ++t) th.emplace_back(work);
+    work();
+    for (auto& x : th) x.join();
+}
+
 // Grouping on the device: off, or on with groupRectangles' minNeighbors and
 // the per-image raw detection limit.
 struct GroupArgs {
@@ -416,12 +454,38 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     // ---- levels and sizes
     std::vector<std::vector<LevelGeom>> geo(nImg);
     int64_t pixBytes = 0, iiElems = 0, imgBytes = 0;
-    std::vector<int64_t> imgOff(nImg, 0);
+    // Host images reach the device at a 16-byte pitch (the integral row pass
+    // reads 16 pixels per load), in one of three ways.  A page-locked image
+    // whose stride is already a multiple of 16 (and below w + 64) is one
+    // contiguous copy at its own stride; the others go at pitch
+    // align_up(w, 16), row by row, unless they add up to kStageImageBytes or
+    // more: then host threads gather every image of the batch into a pinned
+    // buffer in the device layout, moved by one copy (row by row copies of
+    // 256 scenes moved about 16 GB/s).
+    std::vector<int64_t> imgOff(nImg, 0), imgPitch(nImg, 0);
+    std::vector<char> dense(nImg, 0);
+    bool staged = false;
+    if (!onDevice) {
+        int64_t rowwise = 0;
+        for (int i = 0; i < nImg; ++i) {
+            cudaPointerAttributes a{};
+            const bool locked = cudaPointerGetAttributes(&a, ims[i].ptr) == cudaSuccess && a.type == cudaMemoryTypeHost;
+            if (!locked) cudaGetLastError();
+            dense[i] = locked && ims[i].stride % 16 == 0 && ims[i].stride < ims[i].w + 64;
+            if (!dense[i]) rowwise += align_up(static_cast<int64_t>(ims[i].w), 16) * ims[i].h;
+        }
+        staged = rowwise >= kStageImageBytes;
+        if (staged) std::fill(dense.begin(), dense.end(), 0);
+    }
     for (int i = 0; i < nImg; ++i) {
         geo[i] = plan_levels(ims[i].w, ims[i].h, D->winW, D->winH, sf, minObj);
         if (!onDevice) {
             imgOff[i] = imgBytes;
-            imgBytes += align_up(static_cast<int64_t>(ims[i].w), 16) * ims[i].h;
+            imgPitch[i] = dense[i] ? ims[i].stride : align_up(static_cast<int64_t>(ims[i].w), 16);
+            const int64_t bytes = ims[i].h <= 0 ? 0
+                                  : dense[i] ? imgPitch[i] * (ims[i].h - 1) + ims[i].w
+                                             : imgPitch[i] * ims[i].h;
+            imgBytes += align_up(bytes, 16);
         }
         for (const auto& g : geo[i]) {
             if (g.src != -2) pixBytes += align_up(g.w, 16) * g.h;
@@ -504,7 +568,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     const int th = D->cfg.tileRows;
     for (int i = 0; i < nImg; ++i) {
         const uint8_t* base = onDevice ? ims[i].ptr : D->imgs.as<uint8_t>() + imgOff[i];
-        const int64_t baseStride = onDevice ? ims[i].stride : align_up(ims[i].w, 16);
+        const int64_t baseStride = onDevice ? ims[i].stride : imgPitch[i];
         std::vector<const uint8_t*> lp(geo[i].size());
         std::vector<int64_t> ls(geo[i].size());
         for (size_t k = 0; k < geo[i].size(); ++k) {
@@ -618,6 +682,11 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     S.windows = windows;
     S.queuePasses = static_cast<int>(D->queueEnds.size());
 
+    if (staged) {
+        if ((st = D->himgs.ensure(static_cast<size_t>(imgBytes))) != VJ_OK) return st;
+        stage_images(ims, imgOff, D->himgs.as<uint8_t>());
+    }
+
     int64_t hostCap = std::max<int64_t>({int64_t(1) << 16, D->hostHint});
     if (!D->ev0) {
         VJ_CUDA_TRY(cudaEventCreate(&D->ev0));
@@ -684,10 +753,20 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         if ((st = ensure_graph(D, static_cast<size_t>(planBytes))) != VJ_OK) return st;
         VJ_CUDA_TRY(cudaGraphExecMemcpyNodeSetParams1D(D->exec, D->planNode, D->dplan.p, D->hplan.p,
                                                        static_cast<size_t>(planBytes), cudaMemcpyHostToDevice));
-        if (!onDevice)
-            for (int i = 0; i < nImg; ++i)
-                VJ_CUDA_TRY(cudaMemcpy2DAsync(D->imgs.as<uint8_t>() + imgOff[i], align_up(ims[i].w, 16), ims[i].ptr,
-                                              ims[i].stride, ims[i].w, ims[i].h, cudaMemcpyHostToDevice, s));
+        if (staged) {
+            VJ_CUDA_TRY(cudaMemcpyAsync(D->imgs.p, D->himgs.p, static_cast<size_t>(imgBytes), cudaMemcpyHostToDevice, s));
+        } else if (!onDevice) {
+            for (int i = 0; i < nImg; ++i) {
+                if (ims[i].h <= 0 || ims[i].w <= 0) continue;
+                uint8_t* d = D->imgs.as<uint8_t>() + imgOff[i];
+                if (dense[i])
+                    VJ_CUDA_TRY(cudaMemcpyAsync(d, ims[i].ptr, static_cast<size_t>(imgPitch[i] * (ims[i].h - 1) + ims[i].w),
+                                                cudaMemcpyHostToDevice, s));
+                else
+                    VJ_CUDA_TRY(cudaMemcpy2DAsync(d, imgPitch[i], ims[i].ptr, ims[i].stride, ims[i].w, ims[i].h,
+                                                  cudaMemcpyHostToDevice, s));
+            }
+        }
         {
             std::unique_lock<std::mutex> chainLock;
             if (D->chain) {
@@ -865,6 +944,7 @@ int vj_detector_destroy(vj_detector* d) {
     d->hplan.release();
     d->hctrl.release();
     d->hdets.release();
+    d->himgs.release();
     delete d;
     return ok();
 }

@@ -659,11 +659,21 @@ eval_sort_blocked_kernel(const vj_haar_feature* __restrict__ feats, int featBegi
             for (int c = 0; c < kPk; ++c) dg[c] = 0;
 #pragma unroll
             for (int j = 0; j < R; j += 4) {
-                const uint2 four = load_four(src4, pass, tid * R + j, j);
+                // pass 0 takes the sample order: a thread's four keys are
+                // consecutive, one 16-byte load (80 bytes apart across the
+                // warp, so each quarter-warp covers the 32 banks once)
+                uint32_t k[4];
+                if (pass == 0) {
+                    const uint4 k4 = *reinterpret_cast<const uint4*>(keys + tid * R + j);
+                    k[0] = k4.x, k[1] = k4.y, k[2] = k4.z, k[3] = k4.w;
+                } else {
+                    const uint2 four = src4[j / 4];
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) k[h] = keys[((h < 2 ? four.x : four.y) >> (16 * (h & 1))) & 0xFFFFu];
+                }
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    const uint32_t id = ((h < 2 ? four.x : four.y) >> (16 * (h & 1))) & 0xFFFFu;
-                    const uint32_t d = (keys[id] >> shift) & 31u;
+                    const uint32_t d = (k[h] >> shift) & 31u;
                     ccol[(d & 15u) * kCntRow] += 1u << (d & 16u);
                     dg[(j + h) / 6] |= d << (5 * ((j + h) % 6));
                 }

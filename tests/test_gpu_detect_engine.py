@@ -116,6 +116,32 @@ def test_batch_on_device_images(cuda, vj, basic_pool, full_case):
         assert a.tobytes() == b.tobytes()
 
 
+def test_batch_host_copy_forms(cuda, vj, basic_pool, full_case):
+    """Host images reach the device by one contiguous copy (page-locked, stride
+    a multiple of 16), row by row, or gathered into a pinned buffer by host
+    threads (16 MB or more of images that are not contiguous copies): the
+    three forms give the results of the same images on the device."""
+    torch = cuda
+    st, sg, scene, ref = full_case
+    e = engine(vj, basic_pool, st, sg)
+    sizes = [(1920, 1080), (1283, 721), (1600, 912), (1001, 1333), (2048, 1152), (1440, 999), (1920, 1080),
+             (1111, 777), (3840, 2160)]
+    imgs = [scene] + [vj.synth_scene(40 + k, w, h, 3, 24, 200) for k, (w, h) in enumerate(sizes)]
+    assert sum(im.size for im in imgs) >= 16 << 20
+    dev = [torch.from_numpy(im).cuda() for im in imgs]
+    s0, want = e.detectBatch(dev, applyGrouping=False, capPerImage=20000)
+    assert s0 == 0 and want[0].tobytes() == ref.tobytes()
+    keep = [torch.from_numpy(im).pin_memory() for im in imgs]
+    pinned = [t.numpy() for t in keep]
+    # pageable, >= 16 MB: gathered; page-locked: contiguous copies where the
+    # width is a multiple of 16, row by row for the rest (below 16 MB)
+    for batch in (imgs, pinned, pinned[:3] + imgs[3:5], imgs[:2]):
+        s, got = e.detectBatch(batch, applyGrouping=False, capPerImage=20000)
+        assert s == 0
+        for a, b in zip(got, want):
+            assert a.tobytes() == b.tobytes()
+
+
 def test_reserved_arena(cuda, vj, basic_pool, full_case):
     """With a reserved arena every batch is laid out inside it: same results,
     the detector holds no more than the reservation (plus the model and the
