@@ -126,6 +126,7 @@ struct DevPlan {
     int tileStages, deepFrom, qcap, detCap;
     int queueEnd[kMaxQueuePasses];  // stage range of queue pass m: [m ? queueEnd[m-1] : tileStages, queueEnd[m])
     int hostCap;
+    int spreadStumps;  // 1: deep-pass records reordered within blocks (detect.cu spread_banks)
     // Wait tests: when >= 0, this block leaves before the first grid barrier,
     // so the others' wait runs out after barrierTimeoutNs.
     int holdBlock;
@@ -445,8 +446,13 @@ __device__ __forceinline__ float decoded_value_shared(const LevelStump& d, const
 }
 
 // Leaf value of stump k from the window's integral patch in shared memory
-// (corners already converted to float).
-__device__ __forceinline__ float patch_stump_value(const PStumpPlanes& ps, int k, const float* patch, float inv) {
+// (corners already converted to float; element o at patch[PS * o]).  m0
+// masks the first offset: 0x3FF when the record's bits 10-15 of that half
+// hold its position in the stage's block before reordering (detect.cu
+// spread_banks), else 0xFFFF.
+template <int PS>
+__device__ __forceinline__ float patch_stump_value(const PStumpPlanes& ps, int k, const float* patch, float inv,
+                                                   uint32_t m0) {
     const float4 a = __ldg(reinterpret_cast<const float4*>(ps.a + k));
     const uint4 b = __ldg(ps.b + k);
     const uint4 c = __ldg(ps.c + k);
@@ -455,23 +461,24 @@ __device__ __forceinline__ float patch_stump_value(const PStumpPlanes& ps, int k
     // corner_sharing: r1.p0 = r0.p0, r1.p1 = r0.p1, r1.p2 = r0.p2,
     // r1.p3 = r0.p3, r2.p0 = r1.p3, r2.p3 = r0.p3) takes that corner's value
     // instead of a second shared-memory read; the values are the same.
-    const uint32_t o0 = b.z & 0xFFFFu, o1 = b.z >> 16, o2 = b.w & 0xFFFFu, o3 = b.w >> 16;
+    const uint32_t o0 = b.z & m0, o1 = b.z >> 16, o2 = b.w & 0xFFFFu, o3 = b.w >> 16;
     const uint32_t o4 = c.x & 0xFFFFu, o5 = c.x >> 16, o6 = c.y & 0xFFFFu, o7 = c.y >> 16;
-    const float p0 = patch[o0], p1 = patch[o1], p2 = patch[o2], p3 = patch[o3];
+    auto at = [&](uint32_t o) { return patch[PS * o]; };
+    const float p0 = at(o0), p1 = at(o1), p2 = at(o2), p3 = at(o3);
     float p4, p5, p6, p7;
-    if (o4 == o0) p4 = p0; else p4 = patch[o4];
-    if (o5 == o1) p5 = p1; else p5 = patch[o5];
-    if (o6 == o2) p6 = p2; else p6 = patch[o6];
-    if (o7 == o3) p7 = p3; else p7 = patch[o7];
+    if (o4 == o0) p4 = p0; else p4 = at(o4);
+    if (o5 == o1) p5 = p1; else p5 = at(o5);
+    if (o6 == o2) p6 = p2; else p6 = at(o6);
+    if (o7 == o3) p7 = p3; else p7 = at(o7);
     const float v0 = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(p0, p1), p2), p3), a.w);
     const float v1 = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(p4, p5), p6), p7), w1);
     float raw = __fadd_rn(v0, v1);
     if (w2 != 0.0f) {
         const uint32_t o8 = c.z & 0xFFFFu, o9 = c.z >> 16, o10 = c.w & 0xFFFFu, o11 = c.w >> 16;
         float p8, p11;
-        if (o8 == o7) p8 = p7; else p8 = patch[o8];
-        if (o11 == o3) p11 = p3; else p11 = patch[o11];
-        const float v2 = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(p8, patch[o9]), patch[o10]), p11), w2);
+        if (o8 == o7) p8 = p7; else p8 = at(o8);
+        if (o11 == o3) p11 = p3; else p11 = at(o11);
+        const float v2 = __fmul_rn(__fadd_rn(__fsub_rn(__fsub_rn(p8, at(o9)), at(o10)), p11), w2);
         raw = __fadd_rn(raw, v2);
     }
     return __fmul_rn(raw, inv) < a.x ? a.y : a.z;
@@ -721,9 +728,16 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
 // rejected or accepted takes the next window from the queue; the whole warp
 // copies the new window's patch.
 //
-// Per-warp shared memory: 32 * kDeepEvals floats of values, then SL patches.
+// Per-warp shared memory: 32 * kDeepEvals floats of values, then SL patches,
+// element o of slot s at patches[SL * o + s] (two slots interleaved, so their
+// loads fall in different banks: even and odd).  With the stumps of each
+// stage reordered by detect.cu spread_banks, the 16 stumps that one load
+// instruction of a slot reads mostly have distinct o mod 16, i.e. distinct
+// banks; the exact replay puts each value back at the position its stump had
+// before the reordering.
 // ---------------------------------------------------------------------------
 constexpr int kDeepEvals = 3;  // stumps a lane evaluates per step
+constexpr int kDeepBlock = 48; // stumps reordered among themselves (a step of 2 slots; half a step of 1)
 __host__ __device__ constexpr int deep_warp_floats(int slots, int patchElems) {
     return 32 * kDeepEvals + ((slots * patchElems + 3) & ~3);
 }
@@ -733,12 +747,15 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
                                           unsigned long long* workCounter, unsigned long long& evals) {
     constexpr int LPS = 32 / SL;           // lanes per slot
     constexpr int SPS = LPS * kDeepEvals;  // stumps per slot per step
+    static_assert(SPS % kDeepBlock == 0 && LPS % 16 == 0, "steps hold whole reordering blocks of 16-stump groups");
     const int lane = threadIdx.x & 31;
     const int slot = lane / LPS, j = lane % LPS;
-    const int pw = P.winW + 1, ph = P.winH + 1, pe = pw * ph;
+    const int pw = P.winW + 1, ph = P.winH + 1;
     float* vals = wsm;  // per slot SPS values in stump order
     float* patches = wsm + 32 * kDeepEvals;
-    const float* myPatch = patches + slot * pe;
+    const float* myPatch = patches + slot;
+    const bool spread = P.spreadStumps != 0;
+    const uint32_t m0 = spread ? 0x3FFu : 0xFFFFu;
     int qi = -1;  // queue index of the slot's window, -1 = empty
     QEntry e{};
     int si = 0, k0 = 0;
@@ -764,7 +781,7 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
             const uint32_t* sum = L.sum;
             const int64_t Pi = L.pitch;
             const int64_t b = static_cast<int64_t>(ne.xy >> 16) * Pi + static_cast<int64_t>(ne.xy & 0xFFFFu);
-            float* dst = patches + s * pe;
+            float* dst = patches + s;
             // 8 rows' loads in flight before their stores
             for (int c = lane; c < pw; c += 32)
                 for (int r0 = 0; r0 < ph; r0 += 8) {
@@ -774,7 +791,7 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
                         if (r0 + k < ph) v[k] = sum[b + (r0 + k) * Pi + c];
 #pragma unroll
                     for (int k = 0; k < 8; ++k)
-                        if (r0 + k < ph) dst[(r0 + k) * pw + c] = corner_f(v[k]);
+                        if (r0 + k < ph) dst[SL * ((r0 + k) * pw + c)] = corner_f(v[k]);
                 }
             if (slot == s) {
                 qi = static_cast<int>(t);
@@ -796,12 +813,19 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
         for (int ev = 0; ev < kDeepEvals; ++ev) {
             const int k = k0 + ev * LPS + j;
             c[ev] = 0.0f;
-            if (active && k < st.ntrees) c[ev] = patch_stump_value(P.pstumps, st.first + k, myPatch, e.inv);
+            if (active && k < st.ntrees) c[ev] = patch_stump_value<SL>(P.pstumps, st.first + k, myPatch, e.inv, m0);
         }
         const int m = active ? min(SPS, st.ntrees - k0) : 0;
         if (__any_sync(0xffffffffu, exact)) {
 #pragma unroll
-            for (int ev = 0; ev < kDeepEvals; ++ev) vals[slot * SPS + ev * LPS + j] = c[ev];
+            for (int ev = 0; ev < kDeepEvals; ++ev) {
+                int pos = ev * LPS + j;  // k - k0
+                const int k = k0 + pos;
+                if (spread && exact && k < st.ntrees)
+                    pos = k - k % kDeepBlock - k0 +
+                          static_cast<int>((__ldg(&P.pstumps.b[st.first + k].z) >> 10) & 63u);
+                vals[slot * SPS + pos] = c[ev];
+            }
             __syncwarp();
             if (exact) {
                 const float4* v4 = reinterpret_cast<const float4*>(vals + slot * SPS);

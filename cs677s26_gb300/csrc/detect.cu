@@ -173,6 +173,7 @@ struct vj_detector {
     int nStages = 0, nStumps = 0;
     std::vector<DStage> hStages;
     DBuf stumps, pstumps, stages;  // pstumps: planes A, B, C of nStumps uint4 each
+    bool spreadStumps = false;     // the planes are reordered within blocks (spread_banks)
     // Work buffers, grown on demand.
     DBuf imgs, pix, iiSum, iiSq, totS, totQ, qA, qB, dets, dplan, dctrl, ghist;
     HBuf hplan, hctrl, hdets;
@@ -710,6 +711,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         P.detCap = detCap;
         for (size_t m = 0; m < D->queueEnds.size(); ++m) P.queueEnd[m] = D->queueEnds[m];
         P.hostCap = static_cast<int>(std::min<int64_t>(hostCap, INT32_MAX));
+        P.spreadStumps = D->spreadStumps ? 1 : 0;
         P.holdBlock = D->testHoldBlock;
         P.barrierTimeoutNs = D->testBarrierTimeoutNs;
         P.totalTiles = tiles;
@@ -959,6 +961,112 @@ int vj_detector_clear_model(vj_detector* d) {
     return ok();
 }
 
+// Reorders each stage's deep-pass records within blocks of kDeepBlock stumps
+// so that the stumps one deep-pass load instruction reads spread over the
+// shared-memory banks.  Lane j of a slot evaluates stump k0 + 16 ev + j (k0 a
+// multiple of kDeepBlock from the stage's first stump), and the two slots'
+// patches are interleaved (element o of slot s at 2 o + s), so a slot's load
+// of corner c touches bank 2 (o mod 16) + s: one wavefront when the 16 stumps
+// of a group that load corner c have distinct o mod 16.  A seeded local
+// search swaps stumps between the groups of a block while the sum, over
+// groups and corners, of the largest bank count does not grow.  A record
+// keeps its position in the block before the reordering in bits 10-15 of its
+// first offset's half-word (offsets stay below 1024); the deep pass's exact
+// replay adds the values in that order.  Returns false, leaving the order,
+// when the patch has 1,024 elements or more or two stages' stump ranges
+// overlap.
+struct DeepCorners {
+    uint16_t off[12];
+    bool three;  // the third rectangle is evaluated (three rectangles, w2 != 0)
+};
+
+static bool spread_banks(std::vector<uint4>& pa, std::vector<uint4>& pb, std::vector<uint4>& pc,
+                         const std::vector<DeepCorners>& dc, const vj_cascade_stage* stages, int64_t stageCount,
+                         int patchElems) {
+    const int64_t n = static_cast<int64_t>(pa.size());
+    if (patchElems > 1024) return false;
+    std::vector<char> seen(static_cast<size_t>(n), 0);
+    for (int64_t i = 0; i < stageCount; ++i)
+        for (int64_t k = stages[i].first; k < static_cast<int64_t>(stages[i].first) + stages[i].ntrees; ++k) {
+            if (seen[static_cast<size_t>(k)]) return false;
+            seen[static_cast<size_t>(k)] = 1;
+        }
+    // the corners the deep pass reads (patch_stump_value: a corner equal to
+    // an earlier one is not read again)
+    auto loads = [&](int64_t r, int c) {
+        const uint16_t* o = dc[static_cast<size_t>(r)].off;
+        if (c < 4) return true;
+        if (c < 8) return o[c] != o[c - 4];
+        if (!dc[static_cast<size_t>(r)].three) return false;
+        if (c == 8) return o[8] != o[7];
+        if (c == 11) return o[11] != o[3];
+        return true;
+    };
+    uint64_t rng = 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {
+        rng ^= rng << 13;
+        rng ^= rng >> 7;
+        rng ^= rng << 17;
+        return rng;
+    };
+    for (int64_t si = 0; si < stageCount; ++si) {
+        const int64_t first = stages[si].first, nt = stages[si].ntrees;
+        for (int64_t b0 = 0; b0 < nt; b0 += kDeepBlock) {
+            const int len = static_cast<int>(std::min<int64_t>(kDeepBlock, nt - b0));
+            const int ng = (len + 15) / 16;
+            std::vector<int> pos(static_cast<size_t>(len));  // block position -> stump (index in the block)
+            for (int t = 0; t < len; ++t) pos[t] = t;
+            if (ng > 1) {
+                // cnt[(g * 12 + c) * 16 + bank]
+                std::vector<int> cnt(static_cast<size_t>(ng) * 12 * 16, 0);
+                auto add = [&](int g, int r, int dlt) {
+                    for (int c = 0; c < 12; ++c)
+                        if (loads(first + b0 + r, c))
+                            cnt[(static_cast<size_t>(g) * 12 + c) * 16 + (dc[static_cast<size_t>(first + b0 + r)].off[c] & 15)] += dlt;
+                };
+                auto cost = [&](int g) {
+                    int sum = 0;
+                    for (int c = 0; c < 12; ++c) {
+                        const int* q = &cnt[(static_cast<size_t>(g) * 12 + c) * 16];
+                        int m = 0;
+                        for (int bk = 0; bk < 16; ++bk) m = std::max(m, q[bk]);
+                        sum += m;
+                    }
+                    return sum;
+                };
+                for (int t = 0; t < len; ++t) add(t / 16, pos[t], 1);
+                std::vector<int> gc(static_cast<size_t>(ng));
+                for (int g = 0; g < ng; ++g) gc[g] = cost(g);
+                for (int it = 0; it < 1500; ++it) {
+                    const int x = static_cast<int>(next() % static_cast<uint64_t>(len));
+                    const int y = static_cast<int>(next() % static_cast<uint64_t>(len));
+                    const int gx = x / 16, gy = y / 16;
+                    if (gx == gy) continue;
+                    add(gx, pos[x], -1), add(gy, pos[y], -1), add(gx, pos[y], 1), add(gy, pos[x], 1);
+                    const int cx = cost(gx), cy = cost(gy);
+                    if (cx + cy <= gc[gx] + gc[gy]) {
+                        std::swap(pos[x], pos[y]);
+                        gc[gx] = cx, gc[gy] = cy;
+                    } else {
+                        add(gx, pos[y], -1), add(gy, pos[x], -1), add(gx, pos[x], 1), add(gy, pos[y], 1);
+                    }
+                }
+            }
+            std::vector<uint4> ra(pa.begin() + first + b0, pa.begin() + first + b0 + len);
+            std::vector<uint4> rb(pb.begin() + first + b0, pb.begin() + first + b0 + len);
+            std::vector<uint4> rc(pc.begin() + first + b0, pc.begin() + first + b0 + len);
+            for (int t = 0; t < len; ++t) {
+                const size_t at = static_cast<size_t>(first + b0 + t), from = static_cast<size_t>(pos[t]);
+                pa[at] = ra[from];
+                pb[at] = rb[from];
+                pc[at] = rc[from];
+                pb[at].z |= static_cast<uint32_t>(pos[t]) << 10;
+            }
+        }
+    }
+    return true;
+}
+
 int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64_t featureCount,
                           const vj_stump4* stumps, int64_t stumpCount, const vj_cascade_stage* stages,
                           int64_t stageCount) {
@@ -969,6 +1077,7 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
     const int patchElems = (d->winW + 1) * (d->winH + 1);
     std::vector<DStump> ds(static_cast<size_t>(stumpCount));
     std::vector<uint4> pa(static_cast<size_t>(stumpCount)), pb(pa.size()), pc(pa.size());
+    std::vector<DeepCorners> dc(pa.size());
     for (int64_t i = 0; i < stumpCount; ++i) {
         const int32_t fi = float_bits(stumps[i].featureBits);
         if (fi < 0 || fi >= featureCount)
@@ -1004,6 +1113,8 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
         pb[j] = make_uint4(static_cast<uint32_t>(float_bits(rr[1]->w)),
                            static_cast<uint32_t>(float_bits(o.nr == 3 ? rr[2]->w : 0.0f)), ow[0], ow[1]);
         pc[j] = make_uint4(ow[2], ow[3], ow[4], ow[5]);
+        std::memcpy(dc[j].off, off, sizeof(off));
+        dc[j].three = o.nr == 3 && rr[2]->w != 0.0f;
     }
     std::vector<DStage> dst(static_cast<size_t>(stageCount));
     for (int64_t i = 0; i < stageCount; ++i) {
@@ -1030,6 +1141,7 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
     if ((st = d->pstumps.ensure(sizeof(uint4) * 3 * pa.size())) != VJ_OK) return st;
     if ((st = d->stages.ensure(sizeof(DStage) * dst.size())) != VJ_OK) return st;
     VJ_CUDA_TRY(cudaMemcpy(d->stumps.p, ds.data(), sizeof(DStump) * ds.size(), cudaMemcpyHostToDevice));
+    const bool spread = spread_banks(pa, pb, pc, dc, stages, stageCount, patchElems);
     for (int k = 0; k < 3; ++k) {
         const std::vector<uint4>& plane = k == 0 ? pa : (k == 1 ? pb : pc);
         VJ_CUDA_TRY(cudaMemcpy(d->pstumps.as<uint4>() + k * pa.size(), plane.data(), sizeof(uint4) * plane.size(),
@@ -1038,6 +1150,7 @@ int vj_detector_set_model(vj_detector* d, const vj_haar_feature* features, int64
     VJ_CUDA_TRY(cudaMemcpy(d->stages.p, dst.data(), sizeof(DStage) * dst.size(), cudaMemcpyHostToDevice));
     d->nStages = static_cast<int>(stageCount);
     d->nStumps = static_cast<int>(stumpCount);
+    d->spreadStumps = spread;
     d->hStages = dst;
     schedule_passes(d);
     return ok();
