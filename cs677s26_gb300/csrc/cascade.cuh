@@ -56,7 +56,7 @@ struct DStage {
 // One pyramid level of one image, as scanned.
 struct CasLevel {
     const uint32_t* sum;
-    const uint64_t* sq;
+    const uint32_t* sq;  // squared sums modulo 2^32 (integral.cuh IIJobT)
     int64_t pitch;
     int workW, workH, step, scanW, scanH, tilesX;
     int64_t tileBase;
@@ -136,10 +136,10 @@ struct DevPlan {
     const int* rjFirst;         // nResize + 1: resize jobs of chain position p
     const int64_t* rjItems;     // nResize: work items of chain position p
     const ResizeJob* rjobs;
-    const IIJob* iijobs;        // one per level
+    const IIJob32* iijobs;      // one per level
     const CasLevel* levels;
     uint32_t* totS;
-    uint64_t* totQ;
+    uint32_t* totQ;
     const DStump* stumps;
     PStumpPlanes pstumps;
     const DStage* stages;
@@ -299,8 +299,7 @@ __device__ __forceinline__ float window_inv(const CasLevel& L, int x, int y, int
     } else {
         ns = static_cast<double>(static_cast<int32_t>(s0 - s1 - s2 + s3));
     }
-    const uint32_t q = static_cast<uint32_t>(L.sq[o0]) - static_cast<uint32_t>(L.sq[o1]) -
-                       static_cast<uint32_t>(L.sq[o2]) + static_cast<uint32_t>(L.sq[o3]);
+    const uint32_t q = L.sq[o0] - L.sq[o1] - L.sq[o2] + L.sq[o3];
     const double area = static_cast<double>(nw * nh);
     const double nf2 = __dsub_rn(__dmul_rn(area, static_cast<double>(q)), __dmul_rn(ns, ns));
     if (!(nf2 > 0.0)) return 0.0f;

@@ -518,9 +518,9 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             if (!onDevice && (r = D->imgs.ensure(imgBytes)) != VJ_OK) return r;
             if ((r = D->pix.ensure(pixBytes)) != VJ_OK) return r;
             if ((r = D->iiSum.ensure(iiElems * 4)) != VJ_OK) return r;
-            if ((r = D->iiSq.ensure(iiElems * 8)) != VJ_OK) return r;
+            if ((r = D->iiSq.ensure(iiElems * 4)) != VJ_OK) return r;
             if ((r = D->totS.ensure(totElems * 4)) != VJ_OK) return r;
-            if ((r = D->totQ.ensure(totElems * 8)) != VJ_OK) return r;
+            if ((r = D->totQ.ensure(totElems * 4)) != VJ_OK) return r;
             if ((r = D->dets.ensure(detBytes)) != VJ_OK) return r;
             if (histTotal && (r = D->ghist.ensure(static_cast<size_t>(histTotal) * 4)) != VJ_OK) return r;
             if ((r = D->qA.ensure(sizeof(QEntry) * static_cast<size_t>(qcap))) != VJ_OK) return r;
@@ -543,9 +543,9 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         carve(D->imgs, static_cast<size_t>(imgBytes));
         carve(D->pix, static_cast<size_t>(pixBytes));
         carve(D->iiSum, static_cast<size_t>(iiElems) * 4);
-        carve(D->iiSq, static_cast<size_t>(iiElems) * 8);
+        carve(D->iiSq, static_cast<size_t>(iiElems) * 4);
         carve(D->totS, static_cast<size_t>(totElems) * 4);
-        carve(D->totQ, static_cast<size_t>(totElems) * 8);
+        carve(D->totQ, static_cast<size_t>(totElems) * 4);
         carve(D->dets, detBytes);
         if (histTotal) carve(D->ghist, static_cast<size_t>(histTotal) * 4);
         off = static_cast<size_t>(align_up(static_cast<int64_t>(off), 256));
@@ -562,7 +562,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     int st = layout();
     if (st != VJ_OK) return st;
 
-    std::vector<IIJob> iij;
+    std::vector<IIJob32> iij;
     std::vector<CasLevel> lv;
     std::vector<std::vector<ResizeJob>> rj;  // by chain position
     int64_t pixOff = 0, iiOff = 0, tiles = 0, windows = 0, pyrPix = 0;
@@ -601,14 +601,14 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
                 lp[k] = dst;
                 ls[k] = dstStride;
             }
-            IIJob J{};
+            IIJob32 J{};
             J.pix = lp[k];
             J.stride = ls[k];
             J.w = g.w;
             J.h = g.h;
             J.pitch = ii_pitch(g.w);
             J.sum = D->iiSum.as<uint32_t>() + iiOff;
-            J.sq = D->iiSq.as<uint64_t>() + iiOff;
+            J.sq = D->iiSq.as<uint32_t>() + iiOff;
             iiOff += (g.h + 1) * J.pitch;
             iij.push_back(J);
             CasLevel c{};
@@ -653,7 +653,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     const int64_t oItems = align_up(oFirst + sizeof(int) * rjFirst.size(), 64);
     const int64_t oRj = align_up(oItems + sizeof(int64_t) * rjItems.size(), 64);
     const int64_t oII = align_up(oRj + sizeof(ResizeJob) * std::max<size_t>(rjAll.size(), 1), 64);
-    const int64_t oLv = align_up(oII + sizeof(IIJob) * std::max<size_t>(iij.size(), 1), 64);
+    const int64_t oLv = align_up(oII + sizeof(IIJob32) * std::max<size_t>(iij.size(), 1), 64);
     const int64_t oHist = align_up(oLv + sizeof(CasLevel) * std::max<size_t>(lv.size(), 1), 64);
     const int64_t planBytes = align_up(oHist + sizeof(int64_t) * histBase.size(), 64);
     if (planBytes > static_cast<int64_t>(D->dplan.cap) || planBytes > static_cast<int64_t>(D->hplan.cap)) {
@@ -671,7 +671,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     std::memcpy(hp + oFirst, rjFirst.data(), sizeof(int) * rjFirst.size());
     std::memcpy(hp + oItems, rjItems.data(), sizeof(int64_t) * rjItems.size());
     if (!rjAll.empty()) std::memcpy(hp + oRj, rjAll.data(), sizeof(ResizeJob) * rjAll.size());
-    std::memcpy(hp + oII, iij.data(), sizeof(IIJob) * iij.size());
+    std::memcpy(hp + oII, iij.data(), sizeof(IIJob32) * iij.size());
     std::memcpy(hp + oLv, lv.data(), sizeof(CasLevel) * lv.size());
     std::memcpy(hp + oHist, histBase.data(), sizeof(int64_t) * histBase.size());
 
@@ -719,10 +719,10 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         P.rjFirst = reinterpret_cast<const int*>(dp + oFirst);
         P.rjItems = reinterpret_cast<const int64_t*>(dp + oItems);
         P.rjobs = reinterpret_cast<const ResizeJob*>(dp + oRj);
-        P.iijobs = reinterpret_cast<const IIJob*>(dp + oII);
+        P.iijobs = reinterpret_cast<const IIJob32*>(dp + oII);
         P.levels = reinterpret_cast<const CasLevel*>(dp + oLv);
         P.totS = D->totS.as<uint32_t>();
-        P.totQ = D->totQ.as<uint64_t>();
+        P.totQ = D->totQ.as<uint32_t>();
         P.stumps = D->stumps.as<DStump>();
         P.pstumps.a = D->pstumps.as<uint4>();
         P.pstumps.b = P.pstumps.a + D->nStumps;
@@ -1223,11 +1223,11 @@ int vj_detect_estimate_bytes(int winW, int winH, int w, int h, float scaleFactor
     for (const LevelGeom& g : plan_levels(w, h, winW, winH, scaleFactor, minObjectSize)) {
         if (g.src != -2) t += align_up(g.w, 16) * g.h;           // resized level
         const int64_t ii = static_cast<int64_t>(g.h + 1) * ii_pitch(g.w);
-        t += ii * 12;                                              // sums + squared sums
-        t += static_cast<int64_t>(col_segs(g.h)) * col_chunks(g.w) * 32 * 12;  // segment totals
+        t += ii * 8;                                               // sums + squared sums (32-bit)
+        t += static_cast<int64_t>(col_segs(g.h)) * col_chunks(g.w) * 32 * 8;  // segment totals
         const int64_t win = static_cast<int64_t>((g.w - winW + g.step) / g.step) * ((g.h - winH + g.step) / g.step);
         t += 2 * static_cast<int64_t>(sizeof(QEntry)) * (win / 8 + 1);        // two queues
-        t += static_cast<int64_t>(sizeof(CasLevel) + sizeof(IIJob) + sizeof(ResizeJob));
+        t += static_cast<int64_t>(sizeof(CasLevel) + sizeof(IIJob32) + sizeof(ResizeJob));
     }
     t += static_cast<int64_t>(sizeof(vj_detection)) * std::max(64, std::min(std::max(1, maxDetections), 4096));
     *bytes = t + t / 8;  // the work buffers grow with an eighth of slack

@@ -183,22 +183,6 @@ int grid_for(int64_t warps) {
 
 }  // namespace
 
-IIPlan plan_integral_jobs(IIJob* jobs, int njobs) {
-    IIPlan p{0, 0, 0, 0};
-    for (int i = 0; i < njobs; ++i) {
-        IIJob& J = jobs[i];
-        J.rowBase = p.rows;
-        J.itemBase = p.items;
-        J.totBase = p.totRows;
-        p.rows += J.h + 1;
-        p.items += static_cast<int64_t>(col_chunks(J.w)) * col_segs(J.h);
-        p.totRows += col_segs(J.h);
-        const int64_t cols = static_cast<int64_t>(col_chunks(J.w)) * 32;
-        if (cols > p.totPitch) p.totPitch = cols;
-    }
-    return p;
-}
-
 int launch_integral_jobs(const IIJob* d_jobs, int njobs, const IIPlan& plan, uint32_t* d_totS, uint64_t* d_totQ,
                          cudaStream_t stream) {
     if (njobs <= 0) return VJ_OK;

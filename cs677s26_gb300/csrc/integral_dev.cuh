@@ -11,7 +11,8 @@
 
 namespace vjgb {
 
-__device__ __forceinline__ int ii_find_job(const IIJob* __restrict__ jobs, int njobs, int64_t item, bool byRow) {
+template <class Q>
+__device__ __forceinline__ int ii_find_job(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t item, bool byRow) {
     int lo = 0, hi = njobs - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -27,11 +28,12 @@ __device__ __forceinline__ int ii_find_job(const IIJob* __restrict__ jobs, int n
 // Row pass item r: integral row 0 is zero; row y >= 1 holds, at column c, the
 // sum of pixels [0, c) of image row y-1 (and the sum of their squares).
 // 16 pixels per lane, warp shuffle scan, 16-byte stores where aligned.
-__device__ __forceinline__ void ii_row_item(const IIJob* __restrict__ jobs, int njobs, int64_t r, int lane) {
-    const IIJob J = jobs[ii_find_job(jobs, njobs, r, true)];
+template <class Q>
+__device__ __forceinline__ void ii_row_item(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t r, int lane) {
+    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, r, true)];
     const int y = static_cast<int>(r - J.rowBase);
     uint32_t* srow = J.sum + static_cast<size_t>(y) * J.pitch;
-    uint64_t* qrow = J.sq + static_cast<size_t>(y) * J.pitch;
+    Q* qrow = J.sq + static_cast<size_t>(y) * J.pitch;
     const bool vecOut = ((J.pitch & 3) == 0) && ((reinterpret_cast<uintptr_t>(J.sum) & 15) == 0) &&
                         ((reinterpret_cast<uintptr_t>(J.sq) & 15) == 0);
     const uint8_t* prow = y > 0 ? J.pix + static_cast<size_t>(y - 1) * J.stride : nullptr;
@@ -75,26 +77,35 @@ __device__ __forceinline__ void ii_row_item(const IIJob* __restrict__ jobs, int 
         carryQ += __shfl_sync(0xffffffffu, iq, 31);
         if (vecOut && c0 + 15 <= J.w) {
             uint4* so = reinterpret_cast<uint4*>(srow + c0);
-            ulonglong2* qo = reinterpret_cast<ulonglong2*>(qrow + c0);
 #pragma unroll
             for (int i = 0; i < 4; ++i)
                 so[i] = make_uint4(bs + es[4 * i], bs + es[4 * i + 1], bs + es[4 * i + 2], bs + es[4 * i + 3]);
+            if constexpr (sizeof(Q) == 8) {
+                ulonglong2* qo = reinterpret_cast<ulonglong2*>(qrow + c0);
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                qo[i] = make_ulonglong2(static_cast<uint64_t>(bq + eq[2 * i]), static_cast<uint64_t>(bq + eq[2 * i + 1]));
+                for (int i = 0; i < 8; ++i)
+                    qo[i] = make_ulonglong2(static_cast<uint64_t>(bq + eq[2 * i]),
+                                            static_cast<uint64_t>(bq + eq[2 * i + 1]));
+            } else {
+                uint4* qo = reinterpret_cast<uint4*>(qrow + c0);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    qo[i] = make_uint4(bq + eq[4 * i], bq + eq[4 * i + 1], bq + eq[4 * i + 2], bq + eq[4 * i + 3]);
+            }
         } else {
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 if (c0 + i <= J.w) {
                     srow[c0 + i] = bs + es[i];
-                    qrow[c0 + i] = static_cast<uint64_t>(bq + eq[i]);
+                    qrow[c0 + i] = static_cast<Q>(bq + eq[i]);
                 }
             }
         }
     }
 }
 
-__device__ __forceinline__ void ii_col_item(const IIJob& J, int64_t local, int lane, int* seg, int* c, int* r0,
+template <class Q>
+__device__ __forceinline__ void ii_col_item(const IIJobT<Q>& J, int64_t local, int lane, int* seg, int* c, int* r0,
                                             int* r1) {
     const int chunks = (J.w + 1 + 31) >> 5;
     *seg = static_cast<int>(local / chunks);
@@ -105,15 +116,16 @@ __device__ __forceinline__ void ii_col_item(const IIJob& J, int64_t local, int l
 
 // Column pass A item: per 32-row segment and column, the sum of the row
 // prefixes.
-__device__ __forceinline__ void ii_col_total_item(const IIJob* __restrict__ jobs, int njobs, int64_t it, int lane,
+template <class Q>
+__device__ __forceinline__ void ii_col_total_item(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t it, int lane,
                                                   int64_t totPitch, uint32_t* __restrict__ totS,
-                                                  uint64_t* __restrict__ totQ) {
-    const IIJob J = jobs[ii_find_job(jobs, njobs, it, false)];
+                                                  Q* __restrict__ totQ) {
+    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, it, false)];
     int seg, c, r0, r1;
     ii_col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
     if (c > J.w) return;
     uint32_t s = 0;
-    uint64_t q = 0;
+    Q q = 0;
     for (int r = r0; r <= r1; ++r) {
         s += J.sum[static_cast<size_t>(r) * J.pitch + c];
         q += J.sq[static_cast<size_t>(r) * J.pitch + c];
@@ -125,15 +137,16 @@ __device__ __forceinline__ void ii_col_total_item(const IIJob* __restrict__ jobs
 
 // Column pass B item: carry of the segments above, then the running column
 // sum written in place.
-__device__ __forceinline__ void ii_col_scan_item(const IIJob* __restrict__ jobs, int njobs, int64_t it, int lane,
+template <class Q>
+__device__ __forceinline__ void ii_col_scan_item(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t it, int lane,
                                                  int64_t totPitch, const uint32_t* __restrict__ totS,
-                                                 const uint64_t* __restrict__ totQ) {
-    const IIJob J = jobs[ii_find_job(jobs, njobs, it, false)];
+                                                 const Q* __restrict__ totQ) {
+    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, it, false)];
     int seg, c, r0, r1;
     ii_col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
     if (c > J.w) return;
     uint32_t s = 0;
-    uint64_t q = 0;
+    Q q = 0;
     for (int k = 0; k < seg; ++k) {
         const size_t o = static_cast<size_t>(J.totBase + k) * totPitch + c;
         s += totS[o];
