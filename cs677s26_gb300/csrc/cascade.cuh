@@ -127,6 +127,7 @@ struct DevPlan {
     int queueEnd[kMaxQueuePasses];  // stage range of queue pass m: [m ? queueEnd[m-1] : tileStages, queueEnd[m])
     int hostCap;
     int spreadStumps;  // 1: deep-pass records reordered within blocks (detect.cu spread_banks)
+    int colWalk;       // integral column pass: 1 one walk per column chunk, 0 segment totals + scan
     // Wait tests: when >= 0, this block leaves before the first grid barrier,
     // so the others' wait runs out after barrierTimeoutNs.
     int holdBlock;
@@ -138,7 +139,7 @@ struct DevPlan {
     const ResizeJob* rjobs;
     const IIJob32* iijobs;      // one per level
     const CasLevel* levels;
-    uint32_t* totS;
+    uint32_t* totS;             // segment totals of the column passes (colWalk 0)
     uint32_t* totQ;
     const DStump* stumps;
     PStumpPlanes pstumps;
@@ -1149,11 +1150,15 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     // 2. integral images
     for (int64_t r = gw; r < P.ip.rows; r += nw) ii_row_item(P.iijobs, P.nLevels, r, lane);
     if (!grid_barrier(G, epoch, tmo)) return;
-    for (int64_t it = gw; it < P.ip.items; it += nw)
-        ii_col_total_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
-    if (!grid_barrier(G, epoch, tmo)) return;
-    for (int64_t it = gw; it < P.ip.items; it += nw)
-        ii_col_scan_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
+    if (P.colWalk) {
+        for (int64_t it = gw; it < P.ip.walkItems; it += nw) ii_col_walk_item(P.iijobs, P.nLevels, it, lane);
+    } else {
+        for (int64_t it = gw; it < P.ip.items; it += nw)
+            ii_col_total_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
+        if (!grid_barrier(G, epoch, tmo)) return;
+        for (int64_t it = gw; it < P.ip.items; it += nw)
+            ii_col_scan_item(P.iijobs, P.nLevels, it, lane, P.ip.totPitch, P.totS, P.totQ);
+    }
     if (!grid_barrier(G, epoch, tmo)) return;
     if (stamper) G->stamp[2] = global_ns();
 

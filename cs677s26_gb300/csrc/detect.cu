@@ -493,14 +493,22 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             iiElems += (g.h + 1) * ii_pitch(g.w);
         }
     }
-    int64_t totRows = 0, totPitch = 0, windowsAll = 0;
+    int64_t totRows = 0, totPitch = 0, walkItems = 0, windowsAll = 0;
     for (int i = 0; i < nImg; ++i)
         for (const auto& g : geo[i]) {
             totRows += col_segs(g.h);
             totPitch = std::max<int64_t>(totPitch, static_cast<int64_t>(col_chunks(g.w)) * 32);
+            walkItems += col_chunks(g.w);
             windowsAll += static_cast<int64_t>((g.w - D->winW + g.step) / g.step) * ((g.h - D->winH + g.step) / g.step);
         }
-    const int64_t totElems = std::max<int64_t>(1, totRows * totPitch);
+    // Column pass of the integrals: one walk per 32-column chunk down all
+    // rows when there are enough chunks to keep every warp of the grid busy
+    // several times over (16 B per element moved), else segment totals and a
+    // segment scan (32-row segments, enough items for any image; 24 B per
+    // element and a grid barrier more).
+    const int64_t gridWarps = static_cast<int64_t>(sm_count()) * 3 * kCasWarps;
+    const bool colWalk = walkItems >= 4 * gridWarps;
+    const int64_t totElems = colWalk ? 1 : std::max<int64_t>(1, totRows * totPitch);
     // the grouping arrays reuse the queue buffers after the deep pass
     const int64_t grpQ = ga.on ? (D->grpHint * kGroupBytesB + 16 * 256) / static_cast<int64_t>(sizeof(QEntry)) + 1 : 0;
     int64_t qcap =
@@ -711,18 +719,19 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         P.detCap = detCap;
         for (size_t m = 0; m < D->queueEnds.size(); ++m) P.queueEnd[m] = D->queueEnds[m];
         P.hostCap = static_cast<int>(std::min<int64_t>(hostCap, INT32_MAX));
+        P.colWalk = colWalk ? 1 : 0;
         P.spreadStumps = D->spreadStumps ? 1 : 0;
         P.holdBlock = D->testHoldBlock;
         P.barrierTimeoutNs = D->testBarrierTimeoutNs;
         P.totalTiles = tiles;
+        P.totS = D->totS.as<uint32_t>();
+        P.totQ = D->totQ.as<uint32_t>();
         P.ip = ip;
         P.rjFirst = reinterpret_cast<const int*>(dp + oFirst);
         P.rjItems = reinterpret_cast<const int64_t*>(dp + oItems);
         P.rjobs = reinterpret_cast<const ResizeJob*>(dp + oRj);
         P.iijobs = reinterpret_cast<const IIJob32*>(dp + oII);
         P.levels = reinterpret_cast<const CasLevel*>(dp + oLv);
-        P.totS = D->totS.as<uint32_t>();
-        P.totQ = D->totQ.as<uint32_t>();
         P.stumps = D->stumps.as<DStump>();
         P.pstumps.a = D->pstumps.as<uint4>();
         P.pstumps.b = P.pstumps.a + D->nStumps;
@@ -1208,8 +1217,8 @@ int vj_detector_occupancy(vj_detector* d, int* blocksPerSM) {
 int vj_detector_device_bytes(const vj_detector* d, int64_t* bytes) {
     if (!d || !bytes) return set_error(VJ_INVALID_ARG, "vj_detector_device_bytes: null argument");
     int64_t t = 0;
-    for (const DBuf* b : {&d->stumps, &d->pstumps, &d->stages, &d->imgs, &d->pix, &d->iiSum, &d->iiSq, &d->totS,
-                          &d->totQ, &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->ghist, &d->arena})
+    for (const DBuf* b : {&d->stumps, &d->pstumps, &d->stages, &d->imgs, &d->pix, &d->iiSum, &d->iiSq,
+                          &d->totS, &d->totQ, &d->qA, &d->qB, &d->dets, &d->dplan, &d->dctrl, &d->ghist, &d->arena})
         if (!b->view) t += static_cast<int64_t>(b->cap);
     *bytes = t;
     return ok();

@@ -26,6 +26,7 @@ struct IIJobT {
     int64_t rowBase;     // first row item of this job in the row pass
     int64_t itemBase;    // first work item of this job in the column passes
     int64_t totBase;     // first segment-total row of this job
+    int64_t walkBase;    // first item of this job in the column walk (one per 32-column chunk)
 };
 using IIJob = IIJobT<uint64_t>;
 using IIJob32 = IIJobT<uint32_t>;
@@ -37,21 +38,24 @@ inline int col_chunks(int w) { return (w + 1 + 31) / 32; }
 inline int col_segs(int h) { return (h + kColSeg - 1) / kColSeg; }
 
 struct IIPlan {
-    int64_t rows;      // row-pass items
-    int64_t items;     // column-pass items (one warp each)
-    int64_t totRows;   // segment-total rows
-    int64_t totPitch;  // columns per segment-total row
+    int64_t rows;       // row-pass items
+    int64_t items;      // column-pass items (one warp each)
+    int64_t totRows;    // segment-total rows
+    int64_t totPitch;   // columns per segment-total row
+    int64_t walkItems;  // column-walk items (one warp per 32-column chunk)
 };
 
 // Fills the bases of each job and returns the sizes of the passes.
 template <class Q>
 IIPlan plan_integral_jobs(IIJobT<Q>* jobs, int njobs) {
-    IIPlan p{0, 0, 0, 0};
+    IIPlan p{0, 0, 0, 0, 0};
     for (int i = 0; i < njobs; ++i) {
         IIJobT<Q>& J = jobs[i];
         J.rowBase = p.rows;
         J.itemBase = p.items;
         J.totBase = p.totRows;
+        J.walkBase = p.walkItems;
+        p.walkItems += col_chunks(J.w);
         p.rows += J.h + 1;
         p.items += static_cast<int64_t>(col_chunks(J.w)) * col_segs(J.h);
         p.totRows += col_segs(J.h);

@@ -11,12 +11,14 @@
 
 namespace vjgb {
 
+// The job of a work item: by row-pass row (`base` 0), column-pass item (1) or
+// column-walk item (2).
 template <class Q>
-__device__ __forceinline__ int ii_find_job(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t item, bool byRow) {
+__device__ __forceinline__ int ii_find_job(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t item, int base) {
     int lo = 0, hi = njobs - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        const int64_t b = byRow ? jobs[mid].rowBase : jobs[mid].itemBase;
+        const int64_t b = base == 0 ? jobs[mid].rowBase : (base == 1 ? jobs[mid].itemBase : jobs[mid].walkBase);
         if (b <= item)
             lo = mid;
         else
@@ -30,7 +32,7 @@ __device__ __forceinline__ int ii_find_job(const IIJobT<Q>* __restrict__ jobs, i
 // 16 pixels per lane, warp shuffle scan, 16-byte stores where aligned.
 template <class Q>
 __device__ __forceinline__ void ii_row_item(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t r, int lane) {
-    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, r, true)];
+    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, r, 0)];
     const int y = static_cast<int>(r - J.rowBase);
     uint32_t* srow = J.sum + static_cast<size_t>(y) * J.pitch;
     Q* qrow = J.sq + static_cast<size_t>(y) * J.pitch;
@@ -120,7 +122,7 @@ template <class Q>
 __device__ __forceinline__ void ii_col_total_item(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t it, int lane,
                                                   int64_t totPitch, uint32_t* __restrict__ totS,
                                                   Q* __restrict__ totQ) {
-    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, it, false)];
+    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, it, 1)];
     int seg, c, r0, r1;
     ii_col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
     if (c > J.w) return;
@@ -141,7 +143,7 @@ template <class Q>
 __device__ __forceinline__ void ii_col_scan_item(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t it, int lane,
                                                  int64_t totPitch, const uint32_t* __restrict__ totS,
                                                  const Q* __restrict__ totQ) {
-    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, it, false)];
+    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, it, 1)];
     int seg, c, r0, r1;
     ii_col_item(J, it - J.itemBase, lane, &seg, &c, &r0, &r1);
     if (c > J.w) return;
@@ -158,6 +160,47 @@ __device__ __forceinline__ void ii_col_scan_item(const IIJobT<Q>* __restrict__ j
         q += J.sq[o];
         J.sum[o] = s;
         J.sq[o] = q;
+    }
+}
+
+// Column walk item (the detection levels' single column pass): one warp per
+// 32-column chunk of a level, lane c down rows 1..h, adding each row prefix to
+// its running column sums and writing them in place; 16 rows' loads in
+// flight.  The additions are modulo 2^32 (or 2^64), so the sums equal the
+// segment passes' whatever the order.
+template <class Q>
+__device__ __forceinline__ void ii_col_walk_item(const IIJobT<Q>* __restrict__ jobs, int njobs, int64_t it,
+                                                 int lane) {
+    const IIJobT<Q> J = jobs[ii_find_job(jobs, njobs, it, 2)];
+    const int c = static_cast<int>(it - J.walkBase) * 32 + lane;
+    if (c > J.w) return;
+    const int64_t P = J.pitch;
+    uint32_t* ps = J.sum + P + c;
+    Q* pq = J.sq + P + c;
+    uint32_t s = 0;
+    Q q = 0;
+    int r = 1;
+    for (; r + 16 <= J.h + 1; r += 16, ps += 16 * P, pq += 16 * P) {
+        uint32_t a[16];
+        Q b[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            a[k] = ps[k * P];
+            b[k] = pq[k * P];
+        }
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            s += a[k];
+            q += b[k];
+            ps[k * P] = s;
+            pq[k * P] = q;
+        }
+    }
+    for (; r <= J.h; ++r, ps += P, pq += P) {
+        s += *ps;
+        q += *pq;
+        *ps = s;
+        *pq = q;
     }
 }
 

@@ -142,6 +142,20 @@ def test_batch_host_copy_forms(cuda, vj, basic_pool, full_case):
             assert a.tobytes() == b.tobytes()
 
 
+def test_large_batch_column_walk(cuda, vj, basic_pool, full_case):
+    """A batch with enough 32-column chunks (56 scenes of 1920x1080, about
+    17,700 chunks) takes the integral column pass as one walk per chunk down
+    all rows; each image alone takes the segment passes.  Same detections."""
+    st, sg, _, _ = full_case
+    e = engine(vj, basic_pool, st, sg)
+    imgs = [vj.synth_scene(300 + k, 1920, 1080, 4, 24, 200) for k in range(56)]
+    s, batch = e.detectBatch(imgs, applyGrouping=False, capPerImage=20000)
+    assert s == 0
+    for im, got in zip(imgs[::5], batch[::5]):
+        s1, alone = e.detectMultiScale(im, 1920, 1080, 1920, 1.25, 4, 24, 200000, applyGrouping=False)
+        assert s1 == 0 and alone.tobytes() == got.tobytes()
+
+
 def test_reserved_arena(cuda, vj, basic_pool, full_case):
     """With a reserved arena every batch is laid out inside it: same results,
     the detector holds no more than the reservation (plus the model and the
