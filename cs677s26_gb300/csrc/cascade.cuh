@@ -549,13 +549,18 @@ __device__ __forceinline__ int find_level(const CasLevel* __restrict__ levels, i
 // list in shared memory, runs stages [s0, s1) over it 32 windows at a time,
 // and after every stage compacts the survivors with a ballot, so the next
 // stage again runs on full warps.  Survivors go to the next queue, or become
-// detections when s1 is the last stage.
+// detections when s1 is the last stage.  A tile's windows share their level,
+// so its list holds 8-byte entries (position; the reciprocal norm, or the
+// score after the last stage) and 32 * TH of them fit the 16 * TH queue
+// entries of a queue pass: the lists never take more shared memory than the
+// deep pass, whatever TH.
 // ---------------------------------------------------------------------------
 template <int TH>
 __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const QEntry* qin, int qinCount, int s0,
                                           int s1, unsigned long long* workCounter, QEntry* qout, int* qoutCount,
                                           unsigned long long& gated, unsigned long long& evals) {
-    constexpr int kCap = 32 * TH;
+    constexpr int kCapQ = 16 * TH;  // queue entries a list holds
+    uint2* tl = reinterpret_cast<uint2*>(lst);  // tile entries: (y << 16 | x, inv or score bits)
     const int lane = threadIdx.x & 31;
     const bool last = s1 >= P.nStages;
     for (;;) {
@@ -578,22 +583,17 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
                 if (gx < L.scanW && gy < L.scanH) iv = window_inv(L, x, y, P.winW, P.winH, P.normMode);
                 const bool ok = iv != 0.0f;
                 const unsigned m = __ballot_sync(0xffffffffu, ok);
-                if (ok) {
-                    QEntry e;
-                    e.level = static_cast<uint32_t>(li);
-                    e.xy = (static_cast<uint32_t>(y) << 16) | static_cast<uint32_t>(x);
-                    e.inv = iv;
-                    e.score = 0.0f;
-                    lst[count + __popc(m & lanemask_lt())] = e;
-                }
+                if (ok)
+                    tl[count + __popc(m & lanemask_lt())] =
+                        make_uint2((static_cast<uint32_t>(y) << 16) | static_cast<uint32_t>(x), __float_as_uint(iv));
                 count += __popc(m);
             }
             gated += static_cast<unsigned>(count);
         } else {
-            // Entries per take: enough to keep every warp busy, 32 to kCap.
+            // Entries per take: enough to keep every warp busy, 32 to kCapQ.
             const int n = qinCount;
             const int warps = gridDim.x * kCasWarps;
-            const int chunk = min(kCap, max(32, ((n + warps - 1) / warps + 31) & ~31));
+            const int chunk = min(kCapQ, max(32, ((n + warps - 1) / warps + 31) & ~31));
             const int64_t base = static_cast<int64_t>(t) * chunk;
             if (base >= n) break;
             count = static_cast<int>(n - base < chunk ? n - base : chunk);
@@ -623,9 +623,9 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
                         inv[q] = 0.0f;
                         acc[q] = 0.0f;
                         if (q < ng && i < count) {
-                            const QEntry e = lst[i];
-                            b[q] = static_cast<int>(e.xy >> 16) * pitch + static_cast<int>(e.xy & 0xFFFFu);
-                            inv[q] = e.inv;
+                            const uint2 e = tl[i];
+                            b[q] = static_cast<int>(e.x >> 16) * pitch + static_cast<int>(e.x & 0xFFFFu);
+                            inv[q] = __uint_as_float(e.y);
                         }
                     }
                     for (int k = 0; k < st.ntrees; ++k) {
@@ -650,14 +650,14 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
                         if (q >= ng) break;
                         const int i = g0 + 32 * q + lane;
                         const bool act = i < count;
-                        QEntry e{};
-                        if (act) e = lst[i];
+                        uint2 e = make_uint2(0u, 0u);
+                        if (act) e = tl[i];
                         const bool pass = act && !(acc[q] < st.threshold);
                         const unsigned m = __ballot_sync(0xffffffffu, pass);
                         __syncwarp();
                         if (pass) {
-                            e.score = acc[q];
-                            lst[nc + __popc(m & lanemask_lt())] = e;
+                            if (last && si + 1 == s1) e.y = __float_as_uint(acc[q]);  // the detection's score
+                            tl[nc + __popc(m & lanemask_lt())] = e;
                         }
                         nc += __popc(m);
                         __syncwarp();
@@ -698,7 +698,19 @@ __device__ __forceinline__ void lane_pass(const DevPlan& P, QEntry* lst, const Q
             const int i = g + lane;
             const bool act = i < count;
             QEntry e{};
-            if (act) e = lst[i];
+            if (act) {
+                if (tileLevel >= 0) {
+                    const uint2 c = tl[i];
+                    e.level = static_cast<uint32_t>(tileLevel);
+                    e.xy = c.x;
+                    if (last)
+                        e.score = __uint_as_float(c.y);
+                    else
+                        e.inv = __uint_as_float(c.y);
+                } else {
+                    e = lst[i];
+                }
+            }
             if (last)
                 emit_warp(P, e, act);
             else
@@ -1163,7 +1175,7 @@ detect_persistent_kernel(const DevPlan* __restrict__ plan) {
     if (stamper) G->stamp[2] = global_ns();
 
     unsigned long long gated = 0, evals = 0, deepEvals = 0;
-    QEntry* lst = reinterpret_cast<QEntry*>(dsmem) + static_cast<size_t>(wib) * 32 * TH;
+    QEntry* lst = reinterpret_cast<QEntry*>(dsmem) + static_cast<size_t>(wib) * 16 * TH;  // 32 * TH * 8 bytes
 
     // 3. tile pass -> queue 0 (or detections)
     lane_pass<TH>(P, lst, nullptr, 0, 0, P.tileStages, &C->work[0], P.q[0], &C->qcount[0], gated, evals);

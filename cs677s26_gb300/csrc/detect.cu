@@ -270,7 +270,7 @@ const void* kernel_ptr(const vj_detect_config& c) {
 }
 
 size_t smem_bytes(const vj_detector* d, int th) {
-    const size_t lists = static_cast<size_t>(kCasWarps) * 32 * th * sizeof(QEntry);
+    const size_t lists = static_cast<size_t>(kCasWarps) * 32 * th * sizeof(uint2);  // cascade.cuh lane_pass
     const size_t deep = static_cast<size_t>(kCasWarps) *
                         deep_warp_floats(d->cfg.deepSlots, (d->winW + 1) * (d->winH + 1)) * sizeof(float);
     return std::max(lists, deep);

@@ -165,7 +165,7 @@ __device__ __forceinline__ void ii_col_scan_item(const IIJobT<Q>* __restrict__ j
 
 // Column walk item (the detection levels' single column pass): one warp per
 // 32-column chunk of a level, lane c down rows 1..h, adding each row prefix to
-// its running column sums and writing them in place; 16 rows' loads in
+// its running column sums and writing them in place; 8 rows' loads in
 // flight.  The additions are modulo 2^32 (or 2^64), so the sums equal the
 // segment passes' whatever the order.
 template <class Q>
@@ -180,16 +180,16 @@ __device__ __forceinline__ void ii_col_walk_item(const IIJobT<Q>* __restrict__ j
     uint32_t s = 0;
     Q q = 0;
     int r = 1;
-    for (; r + 16 <= J.h + 1; r += 16, ps += 16 * P, pq += 16 * P) {
-        uint32_t a[16];
-        Q b[16];
+    for (; r + 8 <= J.h + 1; r += 8, ps += 8 * P, pq += 8 * P) {
+        uint32_t a[8];
+        Q b[8];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
+        for (int k = 0; k < 8; ++k) {
             a[k] = ps[k * P];
             b[k] = pq[k * P];
         }
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
+        for (int k = 0; k < 8; ++k) {
             s += a[k];
             q += b[k];
             ps[k * P] = s;
