@@ -133,6 +133,7 @@ class FaceVisionEngine:
         call("vj_detector_create", self.win[0], self.win[1], maxImageW, maxImageH, maxDetections, C.byref(h))
         self._h = h
         self._iiSet = None
+        self._out = None  # output records of detectMultiScale, reused between calls
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -188,7 +189,9 @@ class FaceVisionEngine:
         """Returns (status, detections).  `image` is a host numpy array or a CUDA tensor."""
         on_dev = not isinstance(image, np.ndarray)
         cap = capacity if capacity is not None else max(1, min(maxDetections, self.maxDetections))
-        out = np.zeros(cap, dtype=DETECTION)
+        if self._out is None or len(self._out) < cap:
+            self._out = np.empty(cap, dtype=DETECTION)
+        out = self._out
         n = C.c_int()
         st = _capi.status("vj_detect", self._h, ptr(image), imageW, imageH, imageStride, int(on_dev),
                           C.c_float(scaleFactor), minNeighbors, minObjectSize, maxDetections, int(applyGrouping),

@@ -190,7 +190,8 @@ struct vj_detector {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t planNode = nullptr;
-    int graphTH = 0, graphGrid = 0;
+    int graphTH = 0, graphGrid = 0, graphBps = 0;
+    size_t graphPlanBytes = 0;  // size the plan copy node was last given
     const void* graphFn = nullptr;
     size_t graphSmem = 0, graphCtrlBytes = 0;
     void* graphPlan = nullptr;
@@ -330,15 +331,19 @@ int ensure_graph(vj_detector* d, size_t planBytes) {
     const size_t smem = smem_bytes(d, th);
     const size_t cbytes = ctrl_bytes(d->imageCap);
     const void* fn = kernel_ptr(d->cfg);
+    // set on every call: detectors with other window sizes share the kernel
     VJ_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    // the grid follows from (kernel, shared memory, blocksPerSM): a graph
+    // built for the same ones and buffers is replayed without asking again
+    if (d->exec && d->graphFn == fn && d->graphTH == th && d->graphBps == d->cfg.blocksPerSM &&
+        d->graphSmem == smem && d->graphPlan == d->dplan.p && d->graphCtrl == d->dctrl.p &&
+        d->graphCtrlBytes == cbytes && d->graphHCtrl == d->hctrl.p)
+        return VJ_OK;
     int fit = 0;
     VJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, kCasThreads, smem));
     if (fit < 1) return set_error(VJ_RUNTIME_ERROR, "detection kernel does not fit on an SM");
     const int bps = d->cfg.blocksPerSM > 0 ? std::min(d->cfg.blocksPerSM, fit) : fit;
     const int grid = bps * sm_count();
-    if (d->exec && d->graphFn == fn && d->graphTH == th && d->graphGrid == grid && d->graphSmem == smem && d->graphPlan == d->dplan.p &&
-        d->graphCtrl == d->dctrl.p && d->graphCtrlBytes == cbytes && d->graphHCtrl == d->hctrl.p)
-        return VJ_OK;
     drop_graph(d);
     cudaGraph_t g = nullptr;
     VJ_CUDA_TRY(cudaGraphCreate(&g, 0));
@@ -385,6 +390,8 @@ int ensure_graph(vj_detector* d, size_t planBytes) {
     d->graphTH = th;
     d->graphFn = fn;
     d->graphGrid = grid;
+    d->graphBps = d->cfg.blocksPerSM;
+    d->graphPlanBytes = planBytes;
     d->graphSmem = smem;
     d->graphCtrlBytes = cbytes;
     d->graphPlan = d->dplan.p;
@@ -762,8 +769,11 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         }
         std::memcpy(hp, &P, sizeof(P));
         if ((st = ensure_graph(D, static_cast<size_t>(planBytes))) != VJ_OK) return st;
-        VJ_CUDA_TRY(cudaGraphExecMemcpyNodeSetParams1D(D->exec, D->planNode, D->dplan.p, D->hplan.p,
-                                                       static_cast<size_t>(planBytes), cudaMemcpyHostToDevice));
+        if (D->graphPlanBytes != static_cast<size_t>(planBytes)) {
+            VJ_CUDA_TRY(cudaGraphExecMemcpyNodeSetParams1D(D->exec, D->planNode, D->dplan.p, D->hplan.p,
+                                                           static_cast<size_t>(planBytes), cudaMemcpyHostToDevice));
+            D->graphPlanBytes = static_cast<size_t>(planBytes);
+        }
         if (staged) {
             VJ_CUDA_TRY(cudaMemcpyAsync(D->imgs.p, D->himgs.p, static_cast<size_t>(imgBytes), cudaMemcpyHostToDevice, s));
         } else if (!onDevice) {
