@@ -443,6 +443,10 @@ int vj_crop_resize_batch(int nImages, const uint8_t* const* images, const int* w
  * image's result equals vj_detect on that image alone).  All pyramid levels of
  * all images are scanned by one persistent kernel launch, replayed from a
  * captured CUDA graph.  Images are host pointers unless images_on_device.
+ * Host images are read before the call returns: a page-locked image whose
+ * stride is a multiple of 16 is copied as one block; the others, when they
+ * add up to 16 MB or more, are first gathered by host threads into a pinned
+ * buffer of the detector, else copied row by row.
  * out holds n * capPerImage entries (image i at out + i*capPerImage); counts[i]
  * receives image i's count. */
 int vj_detect_batch(vj_detector* d, int n, const uint8_t* const* images,
