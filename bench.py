@@ -384,8 +384,8 @@ def run_gpu(args, rank, world):
     # DRAM bytes (read + write) per feature-sample of one launch, from ncu's
     # dram__bytes counters on the 16,384-feature x 20,000-sample case, scaled
     # to this launch's size.
-    traffic_per_unit = {"sweep_kernel": (713.445632e6 + 3.454464e6) / (16384 * 20000),
-                        "eval_sort_kernel": (225.129728e6 + 672.283648e6) / (16384 * 20000)}
+    traffic_per_unit = {"sweep_kernel": (713.343488e6 + 3.387648e6) / (16384 * 20000),
+                        "eval_sort_kernel": (227.704576e6 + 671.324416e6) / (16384 * 20000)}
     notes = {"sweep_kernel": "streams the resident orders once per round; HBM is its roofline",
              "eval_sort_kernel": "once per stage; an on-chip radix sort bound by the shared-memory pipe "
                                  "(per-thread digit counters, random key gathers and index scatters), its "
@@ -395,7 +395,7 @@ def run_gpu(args, rank, world):
     # feature-sample from ncu's l1tex__data_pipe_lsu_wavefronts_mem_shared.sum on
     # the same 16,384 x 20,000 case, against one wavefront per cycle per SM at the
     # SM clock sampled during the timed steps (a nominal figure, not a measured peak).
-    smem_wavefronts_per_unit = {"eval_sort_kernel": 1225442763 / (16384 * 20000)}
+    smem_wavefronts_per_unit = {"eval_sort_kernel": 1195117053 / (16384 * 20000)}
     clocks = clk.summary()
     sm_mhz = clocks.get("sm_mhz") or 2070.0
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
