@@ -854,41 +854,49 @@ eval_sort_large_kernel(const vj_haar_feature* __restrict__ feats, int featBegin,
 // when the weights are bit for bit what the last vj_round_update left
 // (wShadow) and the active mask is what the last search saw (aShadow), i.e.
 // nothing but that update changed them.
+//
+// One thread per sample over ceil(n / 1024) blocks; each block writes its
+// totals (a fixed shuffle tree) to part[block], and the last block to finish
+// adds the partials in block order, so the totals do not depend on timing.
+struct PrepPartial {
+    double tp, tn;
+    int np, nn, diff, pad;
+};
+constexpr int kPrepMaxBlocks = 64;  // 65,536 samples
+
 __global__ void __launch_bounds__(1024)
 prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
                   const float* __restrict__ weight, int n, float* __restrict__ wsg,
                   RoundParams* __restrict__ prm, const float* __restrict__ wShadow, uint8_t* __restrict__ aShadow,
-                  const PruneState* __restrict__ ps, const int* gate) {
+                  const PruneState* __restrict__ ps, const int* gate, PrepPartial* __restrict__ part,
+                  unsigned int* __restrict__ done) {
     if (gate_closed(gate)) return;
     __shared__ double sp[32], sn[32];
-    __shared__ int cp[32], cn[32];
-    __shared__ int changed;
+    __shared__ int cp[32], cn[32], cd[32];
+    __shared__ bool lastBlock;
     double tp = 0.0, tn = 0.0;
-    int np = 0, nn = 0;
-    if (threadIdx.x == 0) {
-        wsg[n] = 0.0f;  // the zero slot of one-copy orders
-        changed = 0;
-    }
-    __syncthreads();
-    int diff = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int np = 0, nn = 0, diff = 0;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) wsg[n] = 0.0f;  // the zero slot of one-copy orders
+    if (i < n) {
         const bool act = active == nullptr || active[i] != 0;
+        const float wi = weight[i];
         if (wShadow) {
-            diff |= __float_as_uint(weight[i]) != __float_as_uint(wShadow[i]);
+            diff = __float_as_uint(wi) != __float_as_uint(wShadow[i]);
             const uint8_t a = act ? 1 : 0;
             diff |= aShadow[i] != a;
             aShadow[i] = a;
         }
-        const float w = act ? weight[i] : 0.0f;
+        const float w = act ? wi : 0.0f;
         const bool pos = label[i] > 0;
         wsg[i] = pos ? w : -w;
         if (act) {
             if (pos) {
-                tp += static_cast<double>(w);
-                ++np;
+                tp = static_cast<double>(w);
+                np = 1;
             } else {
-                tn += static_cast<double>(w);
-                ++nn;
+                tn = static_cast<double>(w);
+                nn = 1;
             }
         }
     }
@@ -897,6 +905,7 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
         tn += __shfl_down_sync(0xffffffffu, tn, o);
         np += __shfl_down_sync(0xffffffffu, np, o);
         nn += __shfl_down_sync(0xffffffffu, nn, o);
+        diff |= __shfl_down_sync(0xffffffffu, diff, o);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
@@ -904,18 +913,35 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
         sn[warp] = tn;
         cp[warp] = np;
         cn[warp] = nn;
+        cd[warp] = diff;
     }
-    if (diff) changed = 1;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double TP = 0.0, TN = 0.0;
-        int NP = 0, NN = 0;
+        PrepPartial b{0.0, 0.0, 0, 0, 0, 0};
         for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) {
-            TP += sp[k];
-            TN += sn[k];
-            NP += cp[k];
-            NN += cn[k];
+            b.tp += sp[k];
+            b.tn += sn[k];
+            b.np += cp[k];
+            b.nn += cn[k];
+            b.diff |= cd[k];
         }
+        part[blockIdx.x] = b;
+        __threadfence();
+        lastBlock = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (lastBlock && threadIdx.x == 0) {
+        __threadfence();
+        double TP = 0.0, TN = 0.0;
+        int NP = 0, NN = 0, changed = 0;
+        for (int k = 0; k < static_cast<int>(gridDim.x); ++k) {
+            TP += __ldcg(&part[k].tp);
+            TN += __ldcg(&part[k].tn);
+            NP += __ldcg(&part[k].np);
+            NN += __ldcg(&part[k].nn);
+            changed |= __ldcg(&part[k].diff);
+        }
+        *done = 0u;  // ready for the next launch
         const double u = 5.9604644775390625e-08;
         auto gamma = [&](int k) { return static_cast<double>(k) * u / (1.0 - static_cast<double>(k) * u); };
         const double W = TP + TN;
@@ -2171,6 +2197,8 @@ struct vj_trainer {
     int8_t* d_refParity = nullptr;
     int* d_refSplit = nullptr;
     RoundParams* d_prm = nullptr;
+    PrepPartial* d_prepPart = nullptr;  // prep_round_kernel's per-block totals
+    unsigned int* d_prepDone = nullptr; // its count of finished blocks (0 between launches)
     int* d_status = nullptr;
     // Sweep pruning: per-feature lower bounds of the exact best error, the
     // weights as the last round update left them, the active mask as the last
@@ -2236,6 +2264,11 @@ int ensure_round_scratch(vj_trainer* t) {
     }
     t->pruneReset = true;
     if (!t->d_prm) VJ_CUDA_TRY(cudaMalloc(&t->d_prm, sizeof(RoundParams)));
+    if (!t->d_prepPart) {
+        VJ_CUDA_TRY(cudaMalloc(&t->d_prepPart, sizeof(PrepPartial) * kPrepMaxBlocks));
+        VJ_CUDA_TRY(cudaMalloc(&t->d_prepDone, sizeof(unsigned int)));
+        VJ_CUDA_TRY(cudaMemset(t->d_prepDone, 0, sizeof(unsigned int)));
+    }
     if (!t->d_status) VJ_CUDA_TRY(cudaMalloc(&t->d_status, sizeof(int)));
     t->scratchFeat = F;
     t->scratchN = N;
@@ -2337,6 +2370,8 @@ int vj_trainer_destroy(vj_trainer* t) {
     cudaFree(t->d_refParity);
     cudaFree(t->d_refSplit);
     cudaFree(t->d_prm);
+    cudaFree(t->d_prepPart);
+    cudaFree(t->d_prepDone);
     cudaFree(t->d_status);
     cudaFree(t->d_sortKeys);
     cudaFree(t->d_sortIdx);
@@ -2499,8 +2534,9 @@ int vj_stump_search(vj_trainer* t, const uint8_t* d_usedMask, vj_tile_best* d_ou
         t->pruneReset = false;
     }
     VJ_TIMED_LAUNCH("prep_round_kernel", s,
-                    prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, n, t->d_wsg, t->d_prm,
-                                                         t->d_wShadow, t->d_aShadow, t->d_prune, t->d_gate));
+                    prep_round_kernel<<<(n + 1023) / 1024, 1024, 0, s>>>(
+                        t->d_label, t->d_active, t->d_weight, n, t->d_wsg, t->d_prm, t->d_wShadow, t->d_aShadow,
+                        t->d_prune, t->d_gate, t->d_prepPart, t->d_prepDone));
     VJ_LAUNCH_CHECK("prep_round_kernel");
     const bool smemW = n <= kSmemWeightsMax;
     const int sb = t->slotBase;
@@ -2625,8 +2661,9 @@ int vj_trainer_find_thresholds(vj_trainer* t, const float* d_resp, const uint16_
     if (st != VJ_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VJ_TIMED_LAUNCH("prep_round_kernel", s,
-                    prep_round_kernel<<<1, 1024, 0, s>>>(t->d_label, t->d_active, t->d_weight, t->n, t->d_wsg,
-                                                         t->d_prm, nullptr, nullptr, nullptr, nullptr));
+                    prep_round_kernel<<<(t->n + 1023) / 1024, 1024, 0, s>>>(
+                        t->d_label, t->d_active, t->d_weight, t->n, t->d_wsg, t->d_prm, nullptr, nullptr, nullptr,
+                        nullptr, t->d_prepPart, t->d_prepDone));
     VJ_LAUNCH_CHECK("prep_round_kernel");
     VJ_TIMED_LAUNCH("find_thresholds_kernel", s,
                     find_thresholds_kernel<<<div_up(featureCount, 8), 256, 0, s>>>(d_resp, d_sortedIdx, t->n,
