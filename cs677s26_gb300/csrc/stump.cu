@@ -1684,31 +1684,32 @@ __global__ void reduce_tile_best_kernel(const vj_tile_best* __restrict__ in, int
 // depend on scheduling.
 // ---------------------------------------------------------------------------
 // Round update in two kernels with the arithmetic of one 1024-thread block:
-// thread t of 1024 (kRoundUpdateCtas blocks of 256) accumulates, in double and
-// in sample order, the new unnormalised weights of samples t, t+1024, ...
-// (partial t); the normaliser Z is the halving-tree sum of the 1024 partials,
-// and every weight is divided by Z in double.  The second kernel spreads the
-// divisions (FP64, the round's costliest part) over many blocks; each block
-// rebuilds Z from the partials in the same tree order.
-constexpr int kRoundUpdateCtas = 4;
+// partial t of 1024 is the double sum, in sample order, of the new
+// unnormalised weights of samples t, t+1024, ...; the normaliser Z is the
+// halving-tree sum of the 1024 partials, and every weight is divided by Z in
+// double.  The first kernel computes every sample's new weight on its own
+// thread (ceil(n / 1024) blocks of 1024), and the last block to finish adds
+// the partials in that order, one per thread; the second spreads the divisions (FP64) over many
+// blocks, each rebuilding Z from the partials in the same tree order.
 constexpr int kRoundPartials = 1024;
 
 __device__ __forceinline__ bool best_valid(const vj_tile_best& b) { return b.featureIdx >= 0 && isfinite(b.bestErr); }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(1024, 1)
 round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_best* __restrict__ best,
                     const uint32_t* __restrict__ sumT, const float* __restrict__ invNorm,
                     const int8_t* __restrict__ label, const uint8_t* __restrict__ active,
                     const float* __restrict__ weight, float* __restrict__ strong, int n,
                     uint8_t* __restrict__ usedMask, vj_weak_classifier* __restrict__ weakOut,
                     int* __restrict__ status, double* __restrict__ xbuf, double* __restrict__ partials,
-                    PruneState* __restrict__ ps, int* gate) {
+                    PruneState* __restrict__ ps, int* gate, unsigned int* __restrict__ done) {
     if (gate_closed(gate)) return;
     __shared__ vj_haar_feature sfeat;
     __shared__ float sTheta, sLeft, sRight;
     __shared__ double sF;
     __shared__ int sPar, sValid;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;  // partial index, 0..1023
+    __shared__ bool lastBlock;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // sample
     if (threadIdx.x == 0) {
         const vj_tile_best b = *best;
         const bool valid = best_valid(b);
@@ -1752,42 +1753,39 @@ round_update_kernel(const vj_haar_feature* __restrict__ feats, const vj_tile_bes
     const float theta = sTheta, left = sLeft, right = sRight;
     const double F = sF;
     const int par = sPar;
-    double acc = 0.0;
-    // four samples' loads in flight at once; their values are then added to
-    // the partial in sample order, as one sample per step would
-    for (int i0 = t; i0 < n; i0 += 4 * kRoundPartials) {
-        float r[4], sw[4], wt[4];
-        bool act[4];
-        int lab[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int i = i0 + u * kRoundPartials;
-            if (i < n) {
-                r[u] = train_response(f, sumT, n, i, invNorm[i]);
-                sw[u] = strong[i];
-                act[u] = active == nullptr || active[i] != 0;
-                wt[u] = weight[i];
-                lab[u] = label[i];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int i = i0 + u * kRoundPartials;
-            if (i >= n) break;
-            const bool lt = r[u] < theta;
-            strong[i] = __fadd_rn(sw[u], lt ? left : right);
-            if (!act[u]) {
-                xbuf[i] = 0.0;
-                continue;
-            }
+    if (i < n) {
+        const float r = train_response(f, sumT, n, i, invNorm[i]);
+        const bool lt = r < theta;
+        strong[i] = __fadd_rn(strong[i], lt ? left : right);
+        double x = 0.0;
+        if (active == nullptr || active[i] != 0) {
             const int pred = par > 0 ? (lt ? -1 : 1) : (lt ? 1 : -1);
-            double x = static_cast<double>(wt[u]);
-            if (pred != lab[u]) x = x * F;
-            xbuf[i] = x;
-            acc += x;
+            x = static_cast<double>(weight[i]);
+            if (pred != label[i]) x = x * F;
         }
+        xbuf[i] = x;
     }
-    partials[t] = acc;
+    __threadfence();  // this block's xbuf before its count
+    __syncthreads();
+    if (threadIdx.x == 0) lastBlock = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!lastBlock) return;
+    // partial t: samples t, t+1024, ... in order (an inactive sample's +0.0
+    // leaves the sum as it is), eight loads in flight per step
+    __threadfence();
+    for (int t = threadIdx.x; t < kRoundPartials; t += blockDim.x) {
+        double acc = 0.0;
+        for (int i0 = t; i0 < n; i0 += 8 * kRoundPartials) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = i0 + u * kRoundPartials < n ? __ldcg(xbuf + i0 + u * kRoundPartials) : 0.0;
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (i0 + u * kRoundPartials < n) acc += v[u];
+        }
+        partials[t] = acc;
+    }
+    if (threadIdx.x == 0) *done = 0u;  // ready for the next launch
 }
 
 // With wShadow given, the new weights are also written there, and block 0
@@ -2199,6 +2197,7 @@ struct vj_trainer {
     RoundParams* d_prm = nullptr;
     PrepPartial* d_prepPart = nullptr;  // prep_round_kernel's per-block totals
     unsigned int* d_prepDone = nullptr; // its count of finished blocks (0 between launches)
+    unsigned int* d_updDone = nullptr;  // round_update_kernel's count of finished blocks
     int* d_status = nullptr;
     // Sweep pruning: per-feature lower bounds of the exact best error, the
     // weights as the last round update left them, the active mask as the last
@@ -2268,6 +2267,8 @@ int ensure_round_scratch(vj_trainer* t) {
         VJ_CUDA_TRY(cudaMalloc(&t->d_prepPart, sizeof(PrepPartial) * kPrepMaxBlocks));
         VJ_CUDA_TRY(cudaMalloc(&t->d_prepDone, sizeof(unsigned int)));
         VJ_CUDA_TRY(cudaMemset(t->d_prepDone, 0, sizeof(unsigned int)));
+        VJ_CUDA_TRY(cudaMalloc(&t->d_updDone, sizeof(unsigned int)));
+        VJ_CUDA_TRY(cudaMemset(t->d_updDone, 0, sizeof(unsigned int)));
     }
     if (!t->d_status) VJ_CUDA_TRY(cudaMalloc(&t->d_status, sizeof(int)));
     t->scratchFeat = F;
@@ -2372,6 +2373,7 @@ int vj_trainer_destroy(vj_trainer* t) {
     cudaFree(t->d_prm);
     cudaFree(t->d_prepPart);
     cudaFree(t->d_prepDone);
+    cudaFree(t->d_updDone);
     cudaFree(t->d_status);
     cudaFree(t->d_sortKeys);
     cudaFree(t->d_sortIdx);
@@ -2598,10 +2600,10 @@ int vj_round_update(vj_trainer* t, const vj_tile_best* d_best, float* d_strong, 
     if (st != VJ_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VJ_TIMED_LAUNCH("round_update_kernel", s,
-                    round_update_kernel<<<kRoundUpdateCtas, 256, 0, s>>>(
+                    round_update_kernel<<<div_up(t->n, kRoundPartials), kRoundPartials, 0, s>>>(
                         t->d_feat, d_best, t->d_sumT, t->d_invNorm, t->d_label, t->d_active, t->d_weight, d_strong,
                         t->n, d_usedMask, d_weak_out, t->d_status, t->d_xbuf, t->d_partials, t->d_prune,
-                        t->d_gate));
+                        t->d_gate, t->d_updDone));
     VJ_LAUNCH_CHECK("round_update_kernel");
     VJ_TIMED_LAUNCH("round_normalize_kernel", s,
                     round_normalize_kernel<<<std::min(div_up(t->n, 256), 2 * sm_count()), 256, 0, s>>>(
