@@ -463,13 +463,13 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     std::vector<std::vector<LevelGeom>> geo(nImg);
     int64_t pixBytes = 0, iiElems = 0, imgBytes = 0;
     // Host images reach the device at a 16-byte pitch (the integral row pass
-    // reads 16 pixels per load), in one of three ways.  A page-locked image
-    // whose stride is already a multiple of 16 (and below w + 64) is one
-    // contiguous copy at its own stride; the others go at pitch
-    // align_up(w, 16), row by row, unless they add up to kStageImageBytes or
-    // more: then host threads gather every image of the batch into a pinned
-    // buffer in the device layout, moved by one copy (row by row copies of
-    // 256 scenes moved about 16 GB/s).
+    // reads 16 pixels per load), in one of three ways.  An image whose rows
+    // are already at that pitch, or a page-locked one whose stride is a
+    // multiple of 16 (and below w + 64), is one contiguous copy at its own
+    // stride; the others go at pitch align_up(w, 16), row by row, unless they
+    // add up to kStageImageBytes or more: then host threads gather every
+    // image of the batch into a pinned buffer in the device layout, moved by
+    // one copy (row by row copies of 256 scenes moved about 16 GB/s).
     std::vector<int64_t> imgOff(nImg, 0), imgPitch(nImg, 0);
     std::vector<char> dense(nImg, 0);
     bool staged = false;
@@ -479,7 +479,8 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             cudaPointerAttributes a{};
             const bool locked = cudaPointerGetAttributes(&a, ims[i].ptr) == cudaSuccess && a.type == cudaMemoryTypeHost;
             if (!locked) cudaGetLastError();
-            dense[i] = locked && ims[i].stride % 16 == 0 && ims[i].stride < ims[i].w + 64;
+            dense[i] = (locked && ims[i].stride % 16 == 0 && ims[i].stride < ims[i].w + 64) ||
+                       ims[i].stride == align_up(static_cast<int64_t>(ims[i].w), 16);
             if (!dense[i]) rowwise += align_up(static_cast<int64_t>(ims[i].w), 16) * ims[i].h;
         }
         staged = rowwise >= kStageImageBytes;
