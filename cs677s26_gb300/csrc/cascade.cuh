@@ -190,18 +190,22 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned& epoch, unsig
         const unsigned target = epoch * gridDim.x;
         const unsigned long long t0 = global_ns();
         bool ok = true;
+        // one load per spin; the error flag and the time limit are checked
+        // every 32 spins
         for (unsigned it = 0;; ++it) {
             if (ld_acquire_u32(&g->arrive) >= target) break;
-            if (ld_acquire_u32(&g->error) != 0u) {
-                ok = false;
-                break;
+            if ((it & 31u) == 31u) {
+                if (ld_acquire_u32(&g->error) != 0u) {
+                    ok = false;
+                    break;
+                }
+                if (global_ns() - t0 > timeoutNs || it > kBarrierMaxSpins) {
+                    atomicExch(&g->error, 1u);
+                    ok = false;
+                    break;
+                }
             }
-            if ((it & 127u) == 127u && (global_ns() - t0 > timeoutNs || it > kBarrierMaxSpins)) {
-                atomicExch(&g->error, 1u);
-                ok = false;
-                break;
-            }
-            __nanosleep(64);
+            __nanosleep(32);
         }
         if (ok && ld_acquire_u32(&g->error) != 0u) ok = false;
         __threadfence();
