@@ -662,12 +662,18 @@ def run_detect_case(args):
         scene = V.synth_scene(1, 1920, 1080, 40, 24, 300)
         call = lambda: e.detectMultiScale(scene, 1920, 1080, 1920)  # noqa: E731
     elif case.startswith("batch"):
-        k = int(case[5:])
+        # batchN: the first N of the 256 scenes from pageable memory; batchNp:
+        # the same from page-locked memory (as the bench's batch line)
+        pinned = case.endswith("p")
+        k = int(case[5:-1] if pinned else case[5:])
         rng = np.random.default_rng(3)
         scenes = []
         for i in range(k):
             t = rng.random()
             scenes.append(V.synth_scene(1000 + i, int(round(320 * 12 ** t)), int(round(240 * 9 ** t)), 5, 24, 300))
+        if pinned:
+            keep = [torch.from_numpy(sc).pin_memory() for sc in scenes]
+            scenes = [t_.numpy() for t_ in keep]
         call = lambda: e.detectBatch(scenes, capPerImage=4096)  # noqa: E731
     else:
         raise SystemExit(f"unknown detect case {case}")
@@ -783,7 +789,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-detect", action="store_true", help="stump step only")
     ap.add_argument("--quick-detect", action="store_true", help="shorter serving traces")
-    ap.add_argument("--detect-case", default=None, help="run one detection case alone: plain1080 or batchN")
+    ap.add_argument("--detect-case", default=None,
+                    help="run one detection case alone: plain1080, batchN (pageable scenes) or batchNp (page-locked)")
     ap.add_argument("--detect-config", default=None, help="launch shape for --detect-case, as JSON")
     args = ap.parse_args()
     global ROUNDS

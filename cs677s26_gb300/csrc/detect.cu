@@ -408,14 +408,17 @@ struct BatchImage {
 
 constexpr int64_t kStageImageBytes = int64_t(16) << 20;
 
-// Copies the images' rows into `dst` at pitch align_up(w, 16) from offset
-// off[i], on up to 16 host threads taking blocks of about 2 MB of rows.
-void stage_images(const std::vector<BatchImage>& ims, const std::vector<int64_t>& off, uint8_t* dst) {
+// Copies the rows of the images not read in place (skip[i] null) into `dst`
+// at pitch align_up(w, 16) from offset off[i], on up to 16 host threads
+// taking blocks of about 2 MB of rows.
+void stage_images(const std::vector<BatchImage>& ims, const std::vector<int64_t>& off,
+                  const std::vector<const uint8_t*>& skip, uint8_t* dst) {
     struct Piece {
         int img, r0, r1;
     };
     std::vector<Piece> pieces;
     for (int i = 0; i < static_cast<int>(ims.size()); ++i) {
+        if (skip[i]) continue;
         const int rowsPer = std::max(1, static_cast<int>((int64_t(2) << 20) / std::max(1, ims[i].w)));
         for (int r = 0; r < ims[i].h; r += rowsPer) pieces.push_back({i, r, std::min(ims[i].h, r + rowsPer)});
     }
@@ -462,20 +465,35 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     // ---- levels and sizes
     std::vector<std::vector<LevelGeom>> geo(nImg);
     int64_t pixBytes = 0, iiElems = 0, imgBytes = 0;
-    // Host images reach the device at a 16-byte pitch (the integral row pass
-    // reads 16 pixels per load), in one of three ways.  An image whose rows
-    // are already at that pitch, or a page-locked one whose stride is a
-    // multiple of 16 (and below w + 64), is one contiguous copy at its own
-    // stride; the others go at pitch align_up(w, 16), row by row, unless they
-    // add up to kStageImageBytes or more: then host threads gather every
-    // image of the batch into a pinned buffer in the device layout, moved by
-    // one copy (row by row copies of 256 scenes moved about 16 GB/s).
+    // Host images.  When the page-locked images of the call add up to
+    // kStageImageBytes or more, the kernel reads each of them in place through
+    // its mapped device address (over the host link; no copy).  The others
+    // reach the device at a 16-byte pitch (the integral row pass reads 16
+    // pixels per load): an image whose rows are already at that pitch, or a
+    // page-locked one whose stride is a multiple of 16 (and below w + 64), is
+    // one contiguous copy at its own stride; the rest go at pitch
+    // align_up(w, 16), row by row, unless the copied images add up to
+    // kStageImageBytes or more: then host threads gather them into a pinned
+    // buffer in the device layout, moved by one copy (row by row copies of 256
+    // scenes moved about 16 GB/s).
     std::vector<int64_t> imgOff(nImg, 0), imgPitch(nImg, 0);
     std::vector<char> dense(nImg, 0);
+    std::vector<const uint8_t*> mapped(nImg, nullptr);
     bool staged = false;
     if (!onDevice) {
-        int64_t rowwise = 0;
+        int64_t rowwise = 0, lockedBytes = 0;
         for (int i = 0; i < nImg; ++i) {
+            cudaPointerAttributes a{};
+            const bool locked = cudaPointerGetAttributes(&a, ims[i].ptr) == cudaSuccess && a.type == cudaMemoryTypeHost;
+            if (!locked) cudaGetLastError();
+            if (locked && a.devicePointer) {
+                mapped[i] = static_cast<const uint8_t*>(a.devicePointer);
+                lockedBytes += ims[i].stride * ims[i].h;
+            }
+        }
+        if (lockedBytes < kStageImageBytes) std::fill(mapped.begin(), mapped.end(), nullptr);
+        for (int i = 0; i < nImg; ++i) {
+            if (mapped[i]) continue;
             cudaPointerAttributes a{};
             const bool locked = cudaPointerGetAttributes(&a, ims[i].ptr) == cudaSuccess && a.type == cudaMemoryTypeHost;
             if (!locked) cudaGetLastError();
@@ -488,7 +506,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     }
     for (int i = 0; i < nImg; ++i) {
         geo[i] = plan_levels(ims[i].w, ims[i].h, D->winW, D->winH, sf, minObj);
-        if (!onDevice) {
+        if (!onDevice && !mapped[i]) {
             imgOff[i] = imgBytes;
             imgPitch[i] = dense[i] ? ims[i].stride : align_up(static_cast<int64_t>(ims[i].w), 16);
             const int64_t bytes = ims[i].h <= 0 ? 0
@@ -584,8 +602,8 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     int64_t pixOff = 0, iiOff = 0, tiles = 0, windows = 0, pyrPix = 0;
     const int th = D->cfg.tileRows;
     for (int i = 0; i < nImg; ++i) {
-        const uint8_t* base = onDevice ? ims[i].ptr : D->imgs.as<uint8_t>() + imgOff[i];
-        const int64_t baseStride = onDevice ? ims[i].stride : imgPitch[i];
+        const uint8_t* base = onDevice ? ims[i].ptr : (mapped[i] ? mapped[i] : D->imgs.as<uint8_t>() + imgOff[i]);
+        const int64_t baseStride = onDevice || mapped[i] ? ims[i].stride : imgPitch[i];
         std::vector<const uint8_t*> lp(geo[i].size());
         std::vector<int64_t> ls(geo[i].size());
         for (size_t k = 0; k < geo[i].size(); ++k) {
@@ -701,7 +719,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
 
     if (staged) {
         if ((st = D->himgs.ensure(static_cast<size_t>(imgBytes))) != VJ_OK) return st;
-        stage_images(ims, imgOff, D->himgs.as<uint8_t>());
+        stage_images(ims, imgOff, mapped, D->himgs.as<uint8_t>());
     }
 
     int64_t hostCap = std::max<int64_t>({int64_t(1) << 16, D->hostHint});
@@ -779,7 +797,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
             VJ_CUDA_TRY(cudaMemcpyAsync(D->imgs.p, D->himgs.p, static_cast<size_t>(imgBytes), cudaMemcpyHostToDevice, s));
         } else if (!onDevice) {
             for (int i = 0; i < nImg; ++i) {
-                if (ims[i].h <= 0 || ims[i].w <= 0) continue;
+                if (ims[i].h <= 0 || ims[i].w <= 0 || mapped[i]) continue;
                 uint8_t* d = D->imgs.as<uint8_t>() + imgOff[i];
                 if (dense[i])
                     VJ_CUDA_TRY(cudaMemcpyAsync(d, ims[i].ptr, static_cast<size_t>(imgPitch[i] * (ims[i].h - 1) + ims[i].w),
