@@ -1124,7 +1124,8 @@ __device__ __noinline__ int group_phases(const DevPlan& P, GridSync* G, unsigned
 // The persistent detection kernel: every phase of a batch in one cooperative
 // launch, phases separated by grid barriers.
 //   1. pyramid: resize chain positions 0, 1, ... (level k from level k-1);
-//   2. integral images of every level: row pass, column totals, column scan;
+//   2. integral images of every level: row pass, then one column walk per
+//      32-column chunk (large batches) or column totals and a column scan;
 //   3. tile pass (lane-per-window) over every level of every image;
 //   4. lane-per-window queue passes (optional);
 //   5. warp-per-window deep pass over the remaining stages;
