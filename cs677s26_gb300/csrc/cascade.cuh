@@ -10,6 +10,7 @@
 // results equal the reference CPU path bit for bit.
 #pragma once
 
+#include <climits>
 #include <type_traits>
 
 #include "group_dev.cuh"
@@ -108,7 +109,7 @@ struct CtrlHead {
     int rawTotal;                          // raw detections held on the device
     int grpOverflow;                       // the grouping arrays have fewer slots than compactTotal
     int grpError;                          // a union-find retry bound ran out
-    int pad;
+    int clTotal;                           // clusters listed by the grouping (all images)
     // followed by int counts[imageCap] (raw detections per image, counting
     // past detCap), int offsets[imageCap] (start of image i's kept raw
     // detections, in the host buffer and in the grouping slots), int
@@ -1016,31 +1017,57 @@ __device__ __noinline__ int group_phases(const DevPlan& P, GridSync* G, unsigned
     if (!grid_barrier(G, epoch, tmo)) return 0;
 
     // d. similar pairs (similarRects, face_vision_engine.cu:585-616) within
-    // the x reach of the earlier rectangle, joined as found: a warp per
-    // rectangle, its lanes over the later rectangles 32 at a time (x order
-    // ends the scan at the first chunk that reaches past the reach)
-    for (int64_t p = gw; p < keptTotal; p += nw) {
-        const int i = ldl2(GP.image + p);
-        const int end = ldl2(P.offsets + i) + keptOf(i);
-        const int ax = ldl2(GP.x + p), ay = ldl2(GP.y + p), aw = ldl2(GP.w + p), ah = ldl2(GP.h + p);
-        const int reach = __float2int_rz(__fmul_rn(__fmul_rn(GP.eps, static_cast<float>(aw + ah)), 0.5f));
-        for (int q0 = static_cast<int>(p) + 1; q0 < end; q0 += 32) {
-            const int q = q0 + lane;
-            bool past = true, sim = false;
-            if (q < end) {
-                const int bx = ldl2(GP.x + q);
-                past = bx > ax + reach;
-                const int by = ldl2(GP.y + q);
-                if (!past && abs(ay - by) <= reach) {
-                    const int bw = ldl2(GP.w + q), bh = ldl2(GP.h + q);
-                    const int delta = __float2int_rz(
-                        __fmul_rn(__fmul_rn(GP.eps, static_cast<float>(min(aw, bw) + min(ah, bh))), 0.5f));
-                    sim = abs(ax - bx) <= delta && abs(ay - by) <= delta && abs(ax + aw - bx - bw) <= delta &&
-                          abs(ay + ah - by - bh) <= delta;
+    // the x reach of the earlier rectangle, joined as found: a warp per RG
+    // consecutive rectangles (RG = the rectangles per warp, 1 to 32), whose
+    // lanes first load one rectangle each (its box and the end of its
+    // image's range); then, rectangle by rectangle, the lanes go over the
+    // later rectangles 32 at a time (x order ends the scan at the first chunk
+    // that reaches past the reach)
+    const int RG = static_cast<int>(min(static_cast<int64_t>(32), max(static_cast<int64_t>(1), keptTotal / nw)));
+    for (int64_t p0 = gw * RG; p0 < keptTotal; p0 += nw * RG) {
+        const int64_t pl = p0 + lane;
+        int lend = 0, lx = 0, ly = 0, lw = 0, lh = 0;
+        if (lane < RG && pl < keptTotal) {
+            const int li = ldl2(GP.image + pl);
+            lend = ldl2(P.offsets + li) + keptOf(li);
+            lx = ldl2(GP.x + pl), ly = ldl2(GP.y + pl), lw = ldl2(GP.w + pl), lh = ldl2(GP.h + pl);
+        }
+        const int rn = static_cast<int>(min(static_cast<int64_t>(RG), keptTotal - p0));
+        for (int r = 0; r < rn; ++r) {
+            const int64_t p = p0 + r;
+            const int end = __shfl_sync(0xffffffffu, lend, r);
+            const int ax = __shfl_sync(0xffffffffu, lx, r), ay = __shfl_sync(0xffffffffu, ly, r);
+            const int aw = __shfl_sync(0xffffffffu, lw, r), ah = __shfl_sync(0xffffffffu, lh, r);
+            const int reach = __float2int_rz(__fmul_rn(__fmul_rn(GP.eps, static_cast<float>(aw + ah)), 0.5f));
+            // two chunks per step, both loaded before either is tested; once
+            // a chunk holds a rectangle past the reach, every later one is
+            // past it too (x order), so the pairs found are the same
+            for (int q0 = static_cast<int>(p) + 1; q0 < end; q0 += 64) {
+                int bx[2], by[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int q = q0 + 32 * h + lane;
+                    bx[h] = q < end ? ldl2(GP.x + q) : INT_MAX;
+                    by[h] = q < end ? ldl2(GP.y + q) : 0;
                 }
+                bool anyPast = false;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int q = q0 + 32 * h + lane;
+                    const bool past = q >= end || bx[h] > ax + reach;
+                    bool sim = false;
+                    if (!past && abs(ay - by[h]) <= reach) {
+                        const int bw = ldl2(GP.w + q), bh = ldl2(GP.h + q);
+                        const int delta = __float2int_rz(
+                            __fmul_rn(__fmul_rn(GP.eps, static_cast<float>(min(aw, bw) + min(ah, bh))), 0.5f));
+                        sim = abs(ax - bx[h]) <= delta && abs(ay - by[h]) <= delta &&
+                              abs(ax + aw - bx[h] - bw) <= delta && abs(ay + ah - by[h] - bh) <= delta;
+                    }
+                    if (sim && !gf_unite(GP.parent, GP.key, static_cast<int>(p), q)) atomicExch(&C->grpError, 1);
+                    anyPast |= past;
+                }
+                if (__any_sync(0xffffffffu, anyPast)) break;
             }
-            if (sim && !gf_unite(GP.parent, GP.key, static_cast<int>(p), q)) atomicExch(&C->grpError, 1);
-            if (__any_sync(0xffffffffu, past)) break;
         }
     }
     if (!grid_barrier(G, epoch, tmo)) return 0;
@@ -1087,18 +1114,20 @@ __device__ __noinline__ int group_phases(const DevPlan& P, GridSync* G, unsigned
         g.image = i;
         g.key = ldl2(GP.key + r);
         GP.cl[ldl2(P.offsets + i) + c] = g;
+        // the cluster's slot into the list phase h walks (parent, whose
+        // entries no phase after e reads)
+        GP.parent[atomicAdd(&C->clTotal, 1)] = ldl2(P.offsets + i) + c;
     }
     if (!grid_barrier(G, epoch, tmo)) return 0;
 
     // h. containment filter against every other cluster of the image, and
-    // each cluster's rank by first-member key: a warp per cluster
-    for (int64_t p = gw; p < keptTotal; p += nw) {
-        const int i = ldl2(GP.image + p);
-        const int off = ldl2(P.offsets + i);
-        const int k = static_cast<int>(p) - off;
-        const int cc = ldl2(P.ccount + i);
-        if (k >= cc) continue;
-        const GCluster a = ldl2_cluster(GP.cl + p);
+    // each cluster's rank by first-member key: a warp per listed cluster
+    const int clTotal = ld_volatile(&C->clTotal);
+    for (int64_t t = gw; t < clTotal; t += nw) {
+        const int slot = ldl2(GP.parent + t);
+        const GCluster a = ldl2_cluster(GP.cl + slot);
+        const int off = ldl2(P.offsets + a.image), cc = ldl2(P.ccount + a.image);
+        const int k = slot - off;
         int rank = 0;
         bool drop = false;
         for (int j = lane; j < cc; j += 32) {
