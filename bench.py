@@ -46,8 +46,8 @@ NPOS = NNEG = 10000
 ROUNDS = 50
 SEED = 1
 BYTES_PER_ELEM_ROUND = 20  # algorithmic model of the stump search
-# BASELINE's metric; `value` is its stump GB/s part (the stage training step),
-# the served images/s and latencies are under "detect".
+# The headline metric of this path; `value` is its stump GB/s part (the stage
+# training step), the served images/s and latencies are under "detect".
 METRIC = "served images/s + p50/p99 ms vs plain detect at equal dets; stump GB/s"
 DTYPE = "f32 (int32 responses, FP64 renorm)"
 
@@ -122,7 +122,7 @@ def sharded_range(F, rank, world):
 
 def workload_config(F, n, world):
     """The `config` of both arms' JSON lines."""
-    c = {"workload": "full stage training step (BASELINE configs[1]): 10,000+10,000 24x24 patches (seed 1), "
+    c = {"workload": "full stage training step: 10,000+10,000 24x24 patches (seed 1), "
                      "162,336 Basic features, 50 boosting rounds",
          "features": F, "samples": n, "rounds": ROUNDS,
          "parallelism": "one GPU" if world == 1 else f"feature-range shards x{world} (one 16-byte candidate "
@@ -204,9 +204,9 @@ def stump_responses(feat, sumT, inv):
 
 
 def oracle_picks(F, n):
-    """The oracle's 50 picks of this workload (tests/golden/config1_picks.json),
+    """The oracle's 50 picks of this workload (tests/golden/stage_step_picks.json),
     when the step runs the full configuration."""
-    path = ROOT / "tests" / "golden" / "config1_picks.json"
+    path = ROOT / "tests" / "golden" / "stage_step_picks.json"
     if not path.exists():
         return None
     g = json.loads(path.read_text())
@@ -226,7 +226,7 @@ def round_report(V, st, pool):
     from the pick to the runner-up among the exactly replayed candidates (null
     when the pick was the only candidate), and whether the pick (featureIdx,
     FP32 error, theta, parity) equals the oracle's for the same round bit for
-    bit (tests/golden/config1_picks.json)."""
+    bit (tests/golden/stage_step_picks.json)."""
     want = oracle_picks(len(pool), st.n)
     V._capi.call("vj_integral_batch", st.d_p.data_ptr(), 24, 24, 24, st.n, st.sumT.data_ptr(), None,
                  st.inv.data_ptr(), None)

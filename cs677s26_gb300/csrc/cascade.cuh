@@ -871,23 +871,23 @@ __device__ __forceinline__ void deep_pass(const DevPlan& P, float* wsm, const QE
         }
         if (done) {
             // 1 pass, 0 reject, -1 replay the stage exactly
-            int verdict;
+            int outcome;
             if (exact)
-                verdict = acc < st.threshold ? 0 : 1;
+                outcome = acc < st.threshold ? 0 : 1;
             else if (tot < __fsub_rd(st.threshold, st.tol))
-                verdict = 0;
+                outcome = 0;
             else if (tot >= __fadd_ru(st.threshold, st.tol) && si + 1 < P.nStages)
-                verdict = 1;
+                outcome = 1;
             else
-                verdict = -1;
-            if (verdict < 0) {
+                outcome = -1;
+            if (outcome < 0) {
                 exact = true;
                 k0 = 0;
                 acc = 0.0f;
             } else {
                 exact = false;
                 lacc = 0.0f;
-                if (verdict == 0) {
+                if (outcome == 0) {
                     qi = -1;
                 } else {
                     score = acc;  // exact on the last stage, which is always replayed

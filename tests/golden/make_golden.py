@@ -152,13 +152,13 @@ def main() -> None:
     gold["rounds"] = {"seed": 47, "npos": 300, "nneg": 300, "features": mF, "picks": rounds,
                       "patches_sha256": sha(mp)}
 
-    # ---- config 0 (plain small): round 1 over the full Basic pool
+    # ---- 2,000 + 2,000 patches: round 1 over the full Basic pool
     t0 = time.time()
     p0 = V.synth_patches(677, 2000, 2000)
     l0 = np.array([1] * 2000 + [-1] * 2000, np.int8)
     w0 = np.full(4000, np.float32(0.5) / np.float32(2000), np.float32)
     r0 = ref_search(R, np.ascontiguousarray(pool), p0, l0, w0)
-    gold["config0_round1"] = {"patches_sha256": sha(p0), "seconds": round(time.time() - t0, 1), **r0}
+    gold["full_pool_round1_4k"] = {"patches_sha256": sha(p0), "seconds": round(time.time() - t0, 1), **r0}
 
     # ---- detection (raw, scan order) and grouping, small cascade
     st, sg = V.synth_cascade(2, 12, 400)

@@ -1,4 +1,4 @@
-"""Generates tests/golden/config1_picks.json: the 50 stump picks of the full
+"""Generates tests/golden/stage_step_picks.json: the 50 stump picks of the full
 stage training step (10,000 face + 10,000 texture patches of 24x24 from seed
 1, all 162,336 Basic features, uniform initial weights 0.5/10,000, 50
 boosting rounds with the FP64 round update and the stage calibration after
@@ -17,9 +17,9 @@ Per round the fixture stores featureIdx, the FP32 error, theta (as float
 bits), parity, the split position, the FP64 error of the same split, the FP32
 gap to the runner-up feature, the stage calibration's fields, and sha256 of
 the weights and strong scores after the update; plus the final weights and
-strong scores in config1_final.npz.
+strong scores in stage_step_final.npz.
 
-    python tests/golden/make_config1.py [--threads 8] [--ref-rounds 0,1,2,49|all|none]
+    python tests/golden/make_stage_step_picks.py [--threads 8] [--ref-rounds 0,1,2,49|all|none]
 
 Needs about 20 GB of host memory and a few minutes on 8 cores (plus about
 half a minute per reference round).
@@ -140,14 +140,14 @@ def main() -> None:
         print(f"round {r}: feature {rec['featureIdx']} err {b['err']:.7g} (fp64 {b['err64']:.7g}) "
               f"runner-up gap {rec['runner_up_gap_fp32']:.3g}", flush=True)
     sp.close()
-    out = {"about": "config 1 (full stage training step) picks of the oracle's runCpuWeakSearch restatement; "
-                    "see make_config1.py",
+    out = {"about": "full stage training step (10,000 + 10,000 patches, 162,336 Basic features, 50 rounds) "
+                    "picks of the oracle's runCpuWeakSearch restatement; see make_stage_step_picks.py",
            "seed": SEED, "npos": NPOS, "nneg": NNEG, "features": int(len(pool)), "rounds": ROUNDS,
            "min_hit_rate": MIN_HIT, "max_false_alarm": MAX_FA, "patches_sha256": sha(patches),
            "reference_rounds": sorted(ref_rounds), "seconds": round(time.time() - t0, 1), "picks": rounds}
-    (HERE / "config1_picks.json").write_text(json.dumps(out, indent=1) + "\n")
-    np.savez_compressed(HERE / "config1_final.npz", weights=w, strong=strong)
-    print(f"wrote config1_picks.json and config1_final.npz in {time.time() - t0:.0f} s")
+    (HERE / "stage_step_picks.json").write_text(json.dumps(out, indent=1) + "\n")
+    np.savez_compressed(HERE / "stage_step_final.npz", weights=w, strong=strong)
+    print(f"wrote stage_step_picks.json and stage_step_final.npz in {time.time() - t0:.0f} s")
 
 
 if __name__ == "__main__":

@@ -131,7 +131,7 @@ def test_group_rectangles_edge_cases(vj, oracle):
 
 def test_synthetic_inputs_are_deterministic(vj, golden):
     p = vj.synth_patches(677, 2000, 2000)
-    assert hashlib.sha256(p.tobytes()).hexdigest() == golden["config0_round1"]["patches_sha256"]
+    assert hashlib.sha256(p.tobytes()).hexdigest() == golden["full_pool_round1_4k"]["patches_sha256"]
     a = vj.synth_scene(5, 333, 177, 3, 24, 100)
     b = vj.synth_scene(5, 333, 177, 3, 24, 100)
     assert a.tobytes() == b.tobytes()

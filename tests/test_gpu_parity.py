@@ -276,8 +276,8 @@ def test_rounds_match_reference_and_oracle(cuda, vj, oracle, golden, basic_pool)
 
 
 @pytest.mark.slow
-def test_config0_round1_full_pool(cuda, vj, oracle, golden, basic_pool):
-    g = golden["config0_round1"]
+def test_full_pool_round1_4k_full_pool(cuda, vj, oracle, golden, basic_pool):
+    g = golden["full_pool_round1_4k"]
     p = vj.synth_patches(677, 2000, 2000)
     labels = np.array([1] * 2000 + [-1] * 2000, np.int8)
     w = np.full(4000, np.float32(0.5) / np.float32(2000), np.float32)

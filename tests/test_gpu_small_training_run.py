@@ -1,4 +1,4 @@
-"""Config 0 end to end: 2,000 + 2,000 patches (seed 677), a 3-stage cascade
+"""A small training run end to end: 2,000 + 2,000 patches (seed 677), a 3-stage cascade
 trained in the run on the device (1, 2 and 3 rounds over the full 162,336
 Basic pool; main.cu:1955-2348), then integral images of a 640x480 scene with 3
 pasted faces and single-scale detection with that cascade.  Every stump pick,
@@ -11,7 +11,7 @@ from test_gpu_parity import Train, dev
 pytestmark = [pytest.mark.gpu, pytest.mark.slow]
 
 
-def test_config0_cascade_and_single_scale_detect(cuda, vj, oracle, basic_pool):
+def test_three_stage_training_and_single_scale_detect(cuda, vj, oracle, basic_pool):
     torch = cuda
     npos = nneg = 2000
     p = vj.synth_patches(677, npos, nneg)

@@ -1,9 +1,9 @@
 """The full stage training step (10,000 face + 10,000 texture patches of seed
 1, all 162,336 Basic features, uniform initial weights, 50 rounds of search,
 FP64 round update and stage calibration) on the device, against
-tests/golden/config1_picks.json: the oracle's restatement of the reference's
+tests/golden/stage_step_picks.json: the oracle's restatement of the reference's
 runCpuWeakSearch (main.cu:587-682) over the same rounds, some of which
-make_config1.py also checked against the reference's own function.
+make_stage_step_picks.py also checked against the reference's own function.
 
 Every round's pick (featureIdx, FP32 error, theta, parity) must equal the
 fixture's bit for bit, and so must every calibration.  The FP64 update may
@@ -26,10 +26,10 @@ def sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def test_config1_fifty_picks_equal_the_oracle(cuda, vj):
+def test_stage_step_fifty_picks_equal_the_oracle(cuda, vj):
     torch = cuda
-    g = json.loads((GOLDEN / "config1_picks.json").read_text())
-    final = np.load(GOLDEN / "config1_final.npz")
+    g = json.loads((GOLDEN / "stage_step_picks.json").read_text())
+    final = np.load(GOLDEN / "stage_step_final.npz")
     npos, nneg = g["npos"], g["nneg"]
     p = vj.synth_patches(g["seed"], npos, nneg)
     assert sha(p) == g["patches_sha256"]

@@ -85,8 +85,8 @@ def test_rounds_with_fp64_update(oracle, golden, vj, basic_pool):
 
 
 @pytest.mark.slow
-def test_config0_round1_full_pool(oracle, golden, vj, basic_pool):
-    g = golden["config0_round1"]
+def test_full_pool_round1_4k_full_pool(oracle, golden, vj, basic_pool):
+    g = golden["full_pool_round1_4k"]
     p = vj.synth_patches(677, 2000, 2000)
     sums, inv = oracle.train_integrals(p)
     labels = np.array([1] * 2000 + [-1] * 2000, np.int8)
