@@ -479,14 +479,15 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
     std::vector<int64_t> imgOff(nImg, 0), imgPitch(nImg, 0);
     std::vector<char> dense(nImg, 0);
     std::vector<const uint8_t*> mapped(nImg, nullptr);
+    std::vector<char> locked(nImg, 0);
     bool staged = false;
     if (!onDevice) {
         int64_t rowwise = 0, lockedBytes = 0;
         for (int i = 0; i < nImg; ++i) {
             cudaPointerAttributes a{};
-            const bool locked = cudaPointerGetAttributes(&a, ims[i].ptr) == cudaSuccess && a.type == cudaMemoryTypeHost;
-            if (!locked) cudaGetLastError();
-            if (locked && a.devicePointer) {
+            locked[i] = cudaPointerGetAttributes(&a, ims[i].ptr) == cudaSuccess && a.type == cudaMemoryTypeHost;
+            if (!locked[i]) cudaGetLastError();
+            if (locked[i] && a.devicePointer) {
                 mapped[i] = static_cast<const uint8_t*>(a.devicePointer);
                 lockedBytes += ims[i].stride * ims[i].h;
             }
@@ -494,10 +495,7 @@ int execute(vj_detector* D, const std::vector<BatchImage>& ims, bool onDevice, f
         if (lockedBytes < kStageImageBytes) std::fill(mapped.begin(), mapped.end(), nullptr);
         for (int i = 0; i < nImg; ++i) {
             if (mapped[i]) continue;
-            cudaPointerAttributes a{};
-            const bool locked = cudaPointerGetAttributes(&a, ims[i].ptr) == cudaSuccess && a.type == cudaMemoryTypeHost;
-            if (!locked) cudaGetLastError();
-            dense[i] = (locked && ims[i].stride % 16 == 0 && ims[i].stride < ims[i].w + 64) ||
+            dense[i] = (locked[i] && ims[i].stride % 16 == 0 && ims[i].stride < ims[i].w + 64) ||
                        ims[i].stride == align_up(static_cast<int64_t>(ims[i].w), 16);
             if (!dense[i]) rowwise += align_up(static_cast<int64_t>(ims[i].w), 16) * ims[i].h;
         }
