@@ -976,7 +976,7 @@ prep_round_kernel(const int8_t* __restrict__ label, const uint8_t* __restrict__ 
 // 2. Fast sweep: one warp per feature, minimum weighted error to within the
 //    bound used for the window.
 // ---------------------------------------------------------------------------
-constexpr int kSweepChunk = 4;  // features a warp takes from the shared counter at once
+constexpr int kSweepChunk = 2;  // features a warp takes from the shared counter at once
 
 template <bool kSmemW, int TPB>
 __global__ void __launch_bounds__(TPB, 1024 / TPB)
