@@ -1678,19 +1678,16 @@ __global__ void reduce_tile_best_kernel(const vj_tile_best* __restrict__ in, int
 
 // ---------------------------------------------------------------------------
 // AdaBoost round update (main.cu:2082-2166, kernels main.cu:829-906) with FP64
-// alpha/log and renormalisation.  One CTA; each thread owns samples
-// t, t+1024, ... whose FP64 contributions it sums in that order; the 1024
-// partial sums are combined by a fixed halving tree, so the result does not
-// depend on scheduling.
+// alpha/log and renormalisation, in two kernels with the arithmetic of one
+// 1024-thread block: partial t of 1024 is the double sum, in sample order, of
+// the new unnormalised weights of samples t, t+1024, ...; the normaliser Z is
+// the halving-tree sum of the 1024 partials, and every weight is divided by Z
+// in double, so the result does not depend on scheduling.  The first kernel
+// computes every sample's new weight on its own thread (ceil(n / 1024) blocks
+// of 1024), and the last block to finish adds the partials in that order, one
+// per thread; the second spreads the divisions (FP64) over many blocks, each
+// rebuilding Z from the partials in the same tree order.
 // ---------------------------------------------------------------------------
-// Round update in two kernels with the arithmetic of one 1024-thread block:
-// partial t of 1024 is the double sum, in sample order, of the new
-// unnormalised weights of samples t, t+1024, ...; the normaliser Z is the
-// halving-tree sum of the 1024 partials, and every weight is divided by Z in
-// double.  The first kernel computes every sample's new weight on its own
-// thread (ceil(n / 1024) blocks of 1024), and the last block to finish adds
-// the partials in that order, one per thread; the second spreads the divisions (FP64) over many
-// blocks, each rebuilding Z from the partials in the same tree order.
 constexpr int kRoundPartials = 1024;
 
 __device__ __forceinline__ bool best_valid(const vj_tile_best& b) { return b.featureIdx >= 0 && isfinite(b.bestErr); }
